@@ -1,0 +1,561 @@
+// batch.cu -- many independent QPs in one persistent launch.
+//
+// Layout: the QPs are packed block-diagonally.  Every per-QP array (CSR
+// structures, values, vectors) is one slice of a batch-wide array; row
+// pointers hold batch-global positions and column indices are QP-local, so
+// the per-QP view used by the device solver (gb_solver.cuh) is a set of
+// offset pointers.  Structures are built once at setup with the same stable
+// radix-sort transposes as the single-QP path (gb_structure.cuh), for all
+// QPs at once.
+//
+// Execution: a persistent grid of CTAs (SM count x occupancy) pulls QPs from
+// an atomic work queue ordered by decreasing nonzero count (largest first, so
+// the tail of the launch is short); each CTA runs the complete OSQP solve for
+// one QP with block-level barriers only.  No QP ever waits on another, so the
+// launch has no device-wide synchronisation at all.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "osqp_gb300.h"
+#include "osqp_gb300_ext.h"
+#include "gb_solver.cuh"
+#include "gb_structure.cuh"
+
+using T = OSQPFloat;
+using namespace gb;
+
+#define BT_TRY(call)                                                              \
+  do {                                                                            \
+    cudaError_t _e = (call);                                                      \
+    if (_e != cudaSuccess) {                                                      \
+      fprintf(stderr, "osqp_gb300 batch: %s failed: %s (%s:%d)\n", #call,         \
+              cudaGetErrorString(_e), __FILE__, __LINE__);                        \
+      return OSQP_ALGEBRA_LOAD_ERROR;                                             \
+    }                                                                             \
+  } while (0)
+
+namespace gbb {
+
+constexpr int kBatchThreads = 512;
+
+struct BatchInst {
+  int n, m, n_off, m_off;
+  int pt_off, a_off;    // offsets of the QP's triu-P and A entries (input order)
+  int kktL, PL, AL, AtL;
+};
+
+template <typename TT>
+struct BatchArrays {
+  int *Prow, *Pcol, *Pdiag, *Psrc;
+  TT *Pval, *Praw;
+  int *Arow, *Acol, *Asrc, *Atrow, *Atcol;
+  TT *Aval, *Araw, *Atval;
+  TT* vn[16];
+  TT* vm[16];
+  int* ctype;
+  SolverScalars* st;
+  const BatchInst* inst;
+
+  __device__ DevProblem<TT> problem(int k) const {
+    const BatchInst b = inst[k];
+    DevProblem<TT> pr;
+    pr.n = b.n; pr.m = b.m;
+    pr.P = CSR<TT>{Prow + b.n_off, Pcol, Pval, b.n, b.n, b.PL};
+    pr.A = CSR<TT>{Arow + b.m_off, Acol, Aval, b.m, b.n, b.AL};
+    pr.At = CSR<TT>{Atrow + b.n_off, Atcol, Atval, b.n, b.m, b.AtL};
+    pr.Pdiag = Pdiag + b.n_off; pr.Psrc = Psrc; pr.Asrc = Asrc;
+    pr.Praw = Praw; pr.Araw = Araw;
+    const int o = b.n_off, p = b.m_off;
+    pr.q = vn[0] + o; pr.q_in = vn[1] + o; pr.D = vn[2] + o; pr.Dinv = vn[3] + o; pr.x = vn[4] + o;
+    pr.dx = vn[5] + o; pr.xp = vn[6] + o; pr.r = vn[7] + o; pr.p0 = vn[8] + o; pr.p1 = vn[9] + o;
+    pr.Kp = vn[10] + o; pr.yv = vn[11] + o; pr.rhs = vn[12] + o; pr.Minv = vn[13] + o;
+    pr.xo = vn[14] + o; pr.dcert = vn[15] + o; pr.Dt = pr.Kp;
+    pr.l = vm[0] + p; pr.u = vm[1] + p; pr.l_in = vm[2] + p; pr.u_in = vm[3] + p; pr.E = vm[4] + p;
+    pr.Einv = vm[5] + p; pr.rho_vec = vm[6] + p; pr.rho_inv_vec = vm[7] + p; pr.z = vm[8] + p;
+    pr.y = vm[9] + p; pr.dy = vm[10] + p; pr.t = vm[11] + p; pr.yo = vm[12] + p;
+    pr.pcert = vm[13] + p; pr.Et = vm[14] + p;
+    pr.ctype = ctype + p;
+    pr.st = st + k;
+    return pr;
+  }
+};
+
+enum BatchMode : int { kModeSetup = 0, kModeSolve = 1, kModeUpdateVec = 2 };
+
+// Persistent kernel: each CTA pulls QPs from the queue and runs `mode` on them.
+template <typename TT>
+__global__ void __launch_bounds__(kBatchThreads, 2)
+k_batch(BatchArrays<TT> B, DevSettings s, int count, int* queue, const int* order, int mode) {
+  __shared__ GroupShared gsh;
+  __shared__ SolverScalars ssc;
+  __shared__ int s_idx;
+  BlockGroup g{&gsh};
+  for (;;) {
+    if (threadIdx.x == 0) s_idx = atomicAdd(queue, 1);
+    __syncthreads();
+    const int idx = s_idx;
+    if (idx >= count) break;
+    const int k = order[idx];
+    DevProblem<TT> pr = B.problem(k);
+    if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pr.st; }
+    __syncthreads();
+    Solver<TT> S{pr, s, &ssc, B.inst[k].kktL};
+    if (mode == kModeSetup) {
+      S.setup(g);
+    } else if (mode == kModeSolve) {
+      S.solve(g);
+    } else {
+      // new q / l / u from *_in with the QP's existing scaling (osqp_api.c:1184-1257)
+      const TT c = (TT)ssc.c;
+      const bool sc_on = s.scaling != 0;
+      for_each(g, pr.n, [&](int i) { pr.q[i] = sc_on ? (pr.q_in[i] * pr.D[i]) * c : pr.q_in[i]; });
+      for_each(g, pr.m, [&](int j) {
+        pr.l[j] = sc_on ? pr.l_in[j] * pr.E[j] : pr.l_in[j];
+        pr.u[j] = sc_on ? pr.u_in[j] * pr.E[j] : pr.u_in[j];
+      });
+      __syncthreads();
+      if (s.rho_is_vec) {
+        S.set_rho_vec(g);
+        __syncthreads();
+        S.update_precond(g);
+      }
+      if (threadIdx.x == 0) { ssc.status = ST_UNSOLVED; ssc.rho_updates = 0; }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *pr.st = ssc;
+    __syncthreads();
+  }
+}
+
+// ---- structure kernels (one CTA per QP) ----
+// A entries: sort key = batch-global row, plus the entry's local column.
+__global__ void k_batch_A_keys(const BatchInst* inst, int count, const int* Ap_all, const int* ap_off,
+                               const int* Ai, int* keys, int* cols, int* Atrow) {
+  for (int k = blockIdx.x; k < count; k += gridDim.x) {
+    const BatchInst b = inst[k];
+    const int* Ap = Ap_all + ap_off[k];
+    for (int j = threadIdx.x; j < b.n; j += blockDim.x) {
+      Atrow[b.n_off + j] = b.a_off + Ap[j];
+      for (int e = Ap[j]; e < Ap[j + 1]; e++) {
+        keys[b.a_off + e] = b.m_off + Ai[b.a_off + e];
+        cols[b.a_off + e] = j;
+      }
+    }
+  }
+}
+
+// Symmetric expansion of each QP's triu P with keys (global_row << 32 | local_col).
+__global__ void k_batch_P_keys(const BatchInst* inst, int count, const int* Pp_all, const int* pp_off,
+                               const int* Pi, int nnzT_total, unsigned long long* keys, int* src) {
+  for (int k = blockIdx.x; k < count; k += gridDim.x) {
+    const BatchInst b = inst[k];
+    const int* Pp = Pp_all + pp_off[k];
+    for (int j = threadIdx.x; j < b.n; j += blockDim.x) {
+      bool has_diag = false;
+      for (int e = Pp[j]; e < Pp[j + 1]; e++) {
+        const int ge = b.pt_off + e;
+        const int i = Pi[ge];
+        keys[ge] = ((unsigned long long)(b.n_off + i) << 32) | (unsigned)j;
+        src[ge] = ge;
+        if (i == j) {
+          has_diag = true;
+          keys[nnzT_total + ge] = ~0ull;
+          src[nnzT_total + ge] = -1;
+        } else {
+          keys[nnzT_total + ge] = ((unsigned long long)(b.n_off + j) << 32) | (unsigned)i;
+          src[nnzT_total + ge] = ge;
+        }
+      }
+      keys[2 * nnzT_total + b.n_off + j] = has_diag ? ~0ull : (((unsigned long long)(b.n_off + j) << 32) | (unsigned)j);
+      src[2 * nnzT_total + b.n_off + j] = -1;
+    }
+  }
+}
+
+__global__ void k_batch_P_from_sorted(const unsigned long long* keys, int nnzF, int rows, int* col, int* rowptr) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= nnzF; k += gridDim.x * blockDim.x) {
+    if (k < nnzF) col[k] = (int)(keys[k] & 0xffffffffu);   // diagonals: k_batch_P_diag
+    const int prev = (k == 0) ? -1 : (int)(keys[k - 1] >> 32);
+    const int cur = (k == nnzF) ? rows : (int)(keys[k] >> 32);
+    for (int r = prev + 1; r <= cur; r++) rowptr[r] = k;
+  }
+}
+
+// Diagonal positions: for every QP row, the entry whose local column equals the local row.
+__global__ void k_batch_P_diag(const BatchInst* inst, int count, const int* rowptr, const int* col, int* diag) {
+  for (int k = blockIdx.x; k < count; k += gridDim.x) {
+    const BatchInst b = inst[k];
+    for (int i = threadIdx.x; i < b.n; i += blockDim.x) {
+      const int gr = b.n_off + i;
+      for (int e = rowptr[gr]; e < rowptr[gr + 1]; e++)
+        if (col[e] == i) { diag[gr] = e; break; }
+    }
+  }
+}
+
+template <typename TT>
+__global__ void k_batch_check_bounds(const TT* l, const TT* u, long long msum, int* bad) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < msum; j += (long long)gridDim.x * blockDim.x)
+    if (l[j] > u[j]) atomicExch(bad, 1);
+}
+
+struct BatchInfo { int status, iter; double obj, prim, dual; };
+
+__global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out, long long* totals) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+    out[k].status = st[k].status;
+    out[k].iter = st[k].iter;
+    out[k].obj = st[k].obj_val;
+    out[k].prim = st[k].prim_res;
+    out[k].dual = st[k].dual_res;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    long long a = 0, p = 0;
+    for (int k = 0; k < count; k++) { a += st[k].iter; p += st[k].pcg_iters_total; }
+    totals[0] = a; totals[1] = p;
+  }
+}
+
+}  // namespace gbb
+
+using namespace gbb;
+
+struct OSQPBatch_ {
+  int count, device;
+  long long nsum, msum, nnzT, nnzA, nnzPf;
+  cudaStream_t stream;
+  cudaEvent_t ev0, ev1;
+  char* arena;
+  BatchArrays<T> B;
+  BatchInst* d_inst;
+  int* d_order;
+  int* d_queue;
+  int* d_flag;
+  BatchInfo* d_info;
+  long long* d_totals;
+  T *stage_q, *stage_l, *stage_u;
+  DevSettings ds;
+  OSQPSettings settings;
+  int grid;
+  float last_ms;
+  long long last_admm, last_pcg;
+  std::vector<BatchInst> inst;
+};
+
+// settings translation shared with the single-QP engine
+static DevSettings batch_dev_settings(const OSQPSettings* st) {
+  DevSettings d;
+  d.rho = st->rho; d.sigma = st->sigma; d.alpha = st->alpha;
+  d.eps_abs = st->eps_abs; d.eps_rel = st->eps_rel;
+  d.eps_prim_inf = st->eps_prim_inf; d.eps_dual_inf = st->eps_dual_inf;
+  d.cg_tol_fraction = st->cg_tol_fraction;
+  d.adaptive_rho_tolerance = st->adaptive_rho_tolerance;
+  d.adaptive_rho_fraction = st->adaptive_rho_fraction;
+  d.time_limit = st->time_limit;
+  d.infty = (double)OSQP_INFTY;
+  d.zero_deadzone = OSQP_ZERO_DEADZONE;
+  d.scaling = st->scaling; d.rho_is_vec = st->rho_is_vec; d.max_iter = st->max_iter;
+  d.check_termination = st->check_termination;
+  d.adaptive_rho = st->adaptive_rho; d.adaptive_rho_interval = st->adaptive_rho_interval;
+  d.cg_max_iter = st->cg_max_iter; d.cg_tol_reduction = st->cg_tol_reduction;
+  d.cg_precond = (int)st->cg_precond;
+  d.scaled_termination = st->scaled_termination; d.check_dualgap = st->check_dualgap;
+  d.warm_starting = st->warm_starting;
+  return d;
+}
+
+static int run_batch_kernel(OSQPBatch* b, int mode) {
+  BT_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream));
+  k_batch<T><<<b->grid, kBatchThreads, 0, b->stream>>>(b->B, b->ds, b->count, b->d_queue, b->d_order, mode);
+  BT_TRY(cudaGetLastError());
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_cleanup(OSQPBatch* b) {
+  if (!b) return 0;
+  if (b->arena) cudaFree(b->arena);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, const OSQPInt* n, const OSQPInt* m,
+                                          const OSQPInt* Pp, const OSQPInt* Pi, const OSQPFloat* Px,
+                                          const OSQPInt* Ap, const OSQPInt* Ai, const OSQPFloat* Ax,
+                                          const OSQPFloat* q, const OSQPFloat* l, const OSQPFloat* u,
+                                          const OSQPSettings* settings) {
+  if (!batchp || count <= 0 || !n || !m || !Pp || !Ap || !q || !settings) return OSQP_DATA_VALIDATION_ERROR;
+  *batchp = NULL;
+  if (settings->linsys_solver != OSQP_INDIRECT_SOLVER) return OSQP_SETTINGS_VALIDATION_ERROR;
+  if (settings->alpha <= 0 || settings->alpha >= 2 || settings->rho <= 0 || settings->sigma <= 0 ||
+      settings->max_iter <= 0 || settings->adaptive_rho == OSQP_ADAPTIVE_RHO_UPDATE_TIME)
+    return OSQP_SETTINGS_VALIDATION_ERROR;
+  if (cudaSetDevice(settings->device) != cudaSuccess) return OSQP_ALGEBRA_LOAD_ERROR;
+
+  OSQPBatch* b = new OSQPBatch_();
+  b->count = count;
+  b->device = settings->device;
+  b->settings = *settings;
+  OSQPSettings& st = b->settings;
+  st.rho = (OSQPFloat)fmin(fmax((double)st.rho, 1e-6), 1e6);
+  if (st.adaptive_rho == OSQP_ADAPTIVE_RHO_UPDATE_ITERATIONS && st.adaptive_rho_interval == 0)
+    st.adaptive_rho_interval = st.check_termination ? OSQP_ADAPTIVE_RHO_MULTIPLE_TERMINATION * st.check_termination
+                                                    : OSQP_ADAPTIVE_RHO_FIXED;
+  if (st.adaptive_rho == OSQP_ADAPTIVE_RHO_UPDATE_KKT_ERROR && st.adaptive_rho_interval == 0)
+    st.adaptive_rho_interval = 1;
+  b->ds = batch_dev_settings(&st);
+
+  // ---- host-side sizes and offsets ----
+  std::vector<OSQPInt> hn(count), hm(count);
+  if (cudaMemcpy(hn.data(), n, sizeof(OSQPInt) * count, cudaMemcpyDefault) != cudaSuccess ||
+      cudaMemcpy(hm.data(), m, sizeof(OSQPInt) * count, cudaMemcpyDefault) != cudaSuccess) {
+    delete b; return OSQP_DATA_VALIDATION_ERROR;
+  }
+  long long nsum = 0, msum = 0, colptr_len = 0;
+  for (int k = 0; k < count; k++) {
+    if (hn[k] <= 0 || hm[k] < 0) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
+    nsum += hn[k]; msum += hm[k]; colptr_len += hn[k] + 1;
+  }
+  std::vector<OSQPInt> hPp(colptr_len), hAp(colptr_len);
+  if (cudaMemcpy(hPp.data(), Pp, sizeof(OSQPInt) * colptr_len, cudaMemcpyDefault) != cudaSuccess ||
+      cudaMemcpy(hAp.data(), Ap, sizeof(OSQPInt) * colptr_len, cudaMemcpyDefault) != cudaSuccess) {
+    delete b; return OSQP_DATA_VALIDATION_ERROR;
+  }
+  b->inst.resize(count);
+  std::vector<int> pp_off(count), work(count);
+  long long no = 0, mo = 0, pto = 0, ao = 0, co = 0;
+  for (int k = 0; k < count; k++) {
+    BatchInst& I = b->inst[k];
+    I.n = hn[k]; I.m = hm[k]; I.n_off = (int)no; I.m_off = (int)mo; I.pt_off = (int)pto; I.a_off = (int)ao;
+    pp_off[k] = (int)co;
+    const int nT = hPp[co + hn[k]], nA = hAp[co + hn[k]];
+    no += hn[k]; mo += hm[k]; pto += nT; ao += nA; co += hn[k] + 1;
+    work[k] = 2 * nT + 2 * nA + hn[k] + hm[k];
+  }
+  if (pto > INT32_MAX / 2 || ao > INT32_MAX || no > INT32_MAX / 2) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
+  b->nsum = nsum; b->msum = msum; b->nnzT = pto; b->nnzA = ao;
+  // diagonal count of P (host scan of the triu pattern) -> full-P size
+  std::vector<OSQPInt> hPi(pto > 0 ? pto : 1);
+  if (pto && cudaMemcpy(hPi.data(), Pi, sizeof(OSQPInt) * pto, cudaMemcpyDefault) != cudaSuccess) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
+  long long ndiag = 0;
+  for (int k = 0; k < count; k++) {
+    const BatchInst& I = b->inst[k];
+    const OSQPInt* P = hPp.data() + pp_off[k];
+    for (int j = 0; j < I.n; j++) {
+      for (int e = P[j]; e < P[j + 1]; e++) {
+        const OSQPInt r = hPi[I.pt_off + e];
+        if (r > j) { delete b; return OSQP_DATA_VALIDATION_ERROR; }   // P must be upper triangular
+        if (r == j) { ndiag++; break; }
+      }
+    }
+  }
+  b->nnzPf = 2 * pto - 2 * ndiag + nsum;
+  for (int k = 0; k < count; k++) {
+    BatchInst& I = b->inst[k];
+    const OSQPInt* P = hPp.data() + pp_off[k];
+    const OSQPInt* A = hAp.data() + pp_off[k];
+    const long long nT = P[I.n], nA = A[I.n];
+    long long nPf_est = 2 * nT + I.n;  // lane choice only needs the mean row length
+    I.PL = pick_lanes(nPf_est, I.n);
+    I.AL = pick_lanes(nA, I.m);
+    I.AtL = pick_lanes(nA, I.n);
+    I.kktL = pick_lanes(nPf_est + nA, I.n);
+  }
+  std::vector<int> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return work[a] > work[c]; });
+
+  // ---- arena ----
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+    osqp_gb300_batch_cleanup(b); return OSQP_ALGEBRA_LOAD_ERROR;
+  }
+  struct Plan { size_t off = 0; size_t take(size_t bytes) { off = (off + 255) & ~size_t(255); size_t o = off; off += bytes > 0 ? bytes : 1; return o; } } pl;
+  const long long nPf = b->nnzPf;
+  size_t o_Prow = pl.take(sizeof(int) * (nsum + 1)), o_Pcol = pl.take(sizeof(int) * nPf), o_Pdiag = pl.take(sizeof(int) * nsum);
+  size_t o_Psrc = pl.take(sizeof(int) * nPf), o_Pval = pl.take(sizeof(T) * nPf), o_Praw = pl.take(sizeof(T) * pto);
+  size_t o_Arow = pl.take(sizeof(int) * (msum + 1)), o_Acol = pl.take(sizeof(int) * ao), o_Asrc = pl.take(sizeof(int) * ao);
+  size_t o_Atrow = pl.take(sizeof(int) * (nsum + 1)), o_Atcol = pl.take(sizeof(int) * ao);
+  size_t o_Aval = pl.take(sizeof(T) * ao), o_Araw = pl.take(sizeof(T) * ao), o_Atval = pl.take(sizeof(T) * ao);
+  size_t o_vn[16], o_vm[16];
+  for (int k = 0; k < 16; k++) o_vn[k] = pl.take(sizeof(T) * nsum);
+  for (int k = 0; k < 16; k++) o_vm[k] = pl.take(sizeof(T) * msum);
+  size_t o_ctype = pl.take(sizeof(int) * msum), o_st = pl.take(sizeof(SolverScalars) * count);
+  size_t o_inst = pl.take(sizeof(BatchInst) * count), o_order = pl.take(sizeof(int) * count);
+  size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 2);
+  size_t o_sq = pl.take(sizeof(T) * nsum), o_sl = pl.take(sizeof(T) * msum), o_su = pl.take(sizeof(T) * msum);
+  if (cudaMalloc(&b->arena, pl.off) != cudaSuccess) { osqp_gb300_batch_cleanup(b); return OSQP_MEM_ALLOC_ERROR; }
+  char* a = b->arena;
+  cudaStream_t s = b->stream;
+  BT_TRY(cudaMemsetAsync(a, 0, pl.off, s));
+  BatchArrays<T>& B = b->B;
+  B.Prow = (int*)(a + o_Prow); B.Pcol = (int*)(a + o_Pcol); B.Pdiag = (int*)(a + o_Pdiag); B.Psrc = (int*)(a + o_Psrc);
+  B.Pval = (T*)(a + o_Pval); B.Praw = (T*)(a + o_Praw);
+  B.Arow = (int*)(a + o_Arow); B.Acol = (int*)(a + o_Acol); B.Asrc = (int*)(a + o_Asrc);
+  B.Atrow = (int*)(a + o_Atrow); B.Atcol = (int*)(a + o_Atcol);
+  B.Aval = (T*)(a + o_Aval); B.Araw = (T*)(a + o_Araw); B.Atval = (T*)(a + o_Atval);
+  for (int k = 0; k < 16; k++) { B.vn[k] = (T*)(a + o_vn[k]); B.vm[k] = (T*)(a + o_vm[k]); }
+  B.ctype = (int*)(a + o_ctype); B.st = (SolverScalars*)(a + o_st);
+  b->d_inst = (BatchInst*)(a + o_inst); B.inst = b->d_inst;
+  b->d_order = (int*)(a + o_order);
+  b->d_queue = (int*)(a + o_misc); b->d_flag = b->d_queue + 1;
+  b->d_info = (BatchInfo*)(a + o_info); b->d_totals = (long long*)(a + o_tot);
+  b->stage_q = (T*)(a + o_sq); b->stage_l = (T*)(a + o_sl); b->stage_u = (T*)(a + o_su);
+
+  BT_TRY(cudaMemcpyAsync(b->d_inst, b->inst.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice, s));
+  BT_TRY(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  BT_TRY(cudaMemcpyAsync(B.Praw, Px, sizeof(T) * pto, cudaMemcpyDefault, s));
+  BT_TRY(cudaMemcpyAsync(B.Araw, Ax, sizeof(T) * ao, cudaMemcpyDefault, s));
+  BT_TRY(cudaMemcpyAsync(B.vn[1], q, sizeof(T) * nsum, cudaMemcpyDefault, s));
+  if (msum) {
+    BT_TRY(cudaMemcpyAsync(B.vm[2], l, sizeof(T) * msum, cudaMemcpyDefault, s));
+    BT_TRY(cudaMemcpyAsync(B.vm[3], u, sizeof(T) * msum, cudaMemcpyDefault, s));
+  }
+  BT_TRY(cudaMemcpyAsync(B.Atcol, Ai, sizeof(int) * ao, cudaMemcpyDefault, s));
+
+  // ---- device structure build ----
+  int *dPp = nullptr, *dAp = nullptr, *dppoff = nullptr, *dPi = nullptr;
+  BT_TRY(cudaMallocAsync((void**)&dPp, sizeof(int) * colptr_len, s));
+  BT_TRY(cudaMallocAsync((void**)&dAp, sizeof(int) * colptr_len, s));
+  BT_TRY(cudaMallocAsync((void**)&dppoff, sizeof(int) * count, s));
+  BT_TRY(cudaMallocAsync((void**)&dPi, sizeof(int) * (pto > 0 ? pto : 1), s));
+  BT_TRY(cudaMemcpyAsync(dPp, hPp.data(), sizeof(int) * colptr_len, cudaMemcpyHostToDevice, s));
+  BT_TRY(cudaMemcpyAsync(dAp, hAp.data(), sizeof(int) * colptr_len, cudaMemcpyHostToDevice, s));
+  BT_TRY(cudaMemcpyAsync(dppoff, pp_off.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  if (pto) BT_TRY(cudaMemcpyAsync(dPi, hPi.data(), sizeof(int) * pto, cudaMemcpyHostToDevice, s));
+  const int sblocks = std::min(count, 4096);
+  {  // A: stable sort of CSC entries by global row
+    int *keys = nullptr, *keys_out = nullptr, *idx = nullptr, *cols = nullptr;
+    void* tmp = nullptr; size_t tmp_bytes = 0;
+    const long long na = ao > 0 ? ao : 1;
+    BT_TRY(cudaMallocAsync((void**)&keys, sizeof(int) * na, s));
+    BT_TRY(cudaMallocAsync((void**)&keys_out, sizeof(int) * na, s));
+    BT_TRY(cudaMallocAsync((void**)&idx, sizeof(int) * na, s));
+    BT_TRY(cudaMallocAsync((void**)&cols, sizeof(int) * na, s));
+    k_batch_A_keys<<<sblocks, 256, 0, s>>>(b->d_inst, count, dAp, dppoff, B.Atcol, keys, cols, B.Atrow);
+    BT_TRY(cudaMemcpyAsync(B.Atrow + nsum, &ao, sizeof(int), cudaMemcpyHostToDevice, s));
+    if (ao) {
+      k_iota<<<1024, 256, 0, s>>>(idx, (int)ao);
+      const int bits = bits_for((unsigned long long)(msum > 0 ? msum : 1));
+      cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys_out, idx, B.Asrc, (int)ao, 0, bits, s);
+      BT_TRY(cudaMallocAsync(&tmp, tmp_bytes ? tmp_bytes : 1, s));
+      BT_TRY(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys_out, idx, B.Asrc, (int)ao, 0, bits, s));
+      k_gather_int<<<1024, 256, 0, s>>>(cols, B.Asrc, (int)ao, B.Acol);
+      cudaFreeAsync(tmp, s);
+    }
+    k_rowptr_from_sorted<<<(int)std::max(1LL, (ao + 256) / 256), 256, 0, s>>>(keys_out, (int)ao, (int)msum, B.Arow);
+    cudaFreeAsync(keys, s); cudaFreeAsync(keys_out, s); cudaFreeAsync(idx, s); cudaFreeAsync(cols, s);
+  }
+  {  // P: symmetric expansion + 64-bit key sort
+    const long long slots = 2 * pto + nsum;
+    unsigned long long *k_in = nullptr, *k_out = nullptr;
+    int *s_in = nullptr;
+    void* tmp = nullptr; size_t tmp_bytes = 0;
+    BT_TRY(cudaMallocAsync((void**)&k_in, sizeof(unsigned long long) * slots, s));
+    BT_TRY(cudaMallocAsync((void**)&k_out, sizeof(unsigned long long) * slots, s));
+    BT_TRY(cudaMallocAsync((void**)&s_in, sizeof(int) * slots, s));
+    int* s_out = nullptr;
+    BT_TRY(cudaMallocAsync((void**)&s_out, sizeof(int) * slots, s));
+    k_batch_P_keys<<<sblocks, 256, 0, s>>>(b->d_inst, count, dPp, dppoff, dPi, (int)pto, k_in, s_in);
+    cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k_in, k_out, s_in, s_out, (int)slots, 0, 64, s);
+    BT_TRY(cudaMallocAsync(&tmp, tmp_bytes ? tmp_bytes : 1, s));
+    BT_TRY(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k_in, k_out, s_in, s_out, (int)slots, 0, 64, s));
+    k_batch_P_from_sorted<<<(int)((nPf + 256) / 256), 256, 0, s>>>(k_out, (int)nPf, (int)nsum, B.Pcol, B.Prow);
+    BT_TRY(cudaMemcpyAsync(B.Psrc, s_out, sizeof(int) * nPf, cudaMemcpyDeviceToDevice, s));
+    k_batch_P_diag<<<sblocks, 256, 0, s>>>(b->d_inst, count, B.Prow, B.Pcol, B.Pdiag);
+    cudaFreeAsync(tmp, s); cudaFreeAsync(k_in, s); cudaFreeAsync(k_out, s); cudaFreeAsync(s_in, s); cudaFreeAsync(s_out, s);
+  }
+  cudaFreeAsync(dPp, s); cudaFreeAsync(dAp, s); cudaFreeAsync(dppoff, s); cudaFreeAsync(dPi, s);
+
+  // ---- persistent grid: SMs x resident CTAs ----
+  int per_sm = 0, sms = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<T>, kBatchThreads, 0);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  b->grid = std::max(1, std::min(count, sms * std::max(per_sm, 1)));
+
+  int rc = run_batch_kernel(b, kModeSetup);
+  if (rc) { osqp_gb300_batch_cleanup(b); return rc; }
+  if (cudaStreamSynchronize(s) != cudaSuccess) { osqp_gb300_batch_cleanup(b); return OSQP_ALGEBRA_LOAD_ERROR; }
+  *batchp = b;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_update_data_vec(OSQPBatch* b, const OSQPFloat* q, const OSQPFloat* l,
+                                                    const OSQPFloat* u) {
+  if (!b) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  cudaSetDevice(b->device);
+  cudaStream_t s = b->stream;
+  BatchArrays<T>& B = b->B;
+  if (l || u) {
+    BT_TRY(cudaMemcpyAsync(b->stage_l, l ? (const void*)l : (const void*)B.vm[2], sizeof(T) * b->msum,
+                           l ? cudaMemcpyDefault : cudaMemcpyDeviceToDevice, s));
+    BT_TRY(cudaMemcpyAsync(b->stage_u, u ? (const void*)u : (const void*)B.vm[3], sizeof(T) * b->msum,
+                           u ? cudaMemcpyDefault : cudaMemcpyDeviceToDevice, s));
+    BT_TRY(cudaMemsetAsync(b->d_flag, 0, sizeof(int), s));
+    k_batch_check_bounds<T><<<1024, 256, 0, s>>>(b->stage_l, b->stage_u, b->msum, b->d_flag);
+    int bad = 0;
+    BT_TRY(cudaMemcpyAsync(&bad, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BT_TRY(cudaStreamSynchronize(s));
+    if (bad) return OSQP_DATA_VALIDATION_ERROR;
+    BT_TRY(cudaMemcpyAsync(B.vm[2], b->stage_l, sizeof(T) * b->msum, cudaMemcpyDeviceToDevice, s));
+    BT_TRY(cudaMemcpyAsync(B.vm[3], b->stage_u, sizeof(T) * b->msum, cudaMemcpyDeviceToDevice, s));
+  }
+  if (q) BT_TRY(cudaMemcpyAsync(B.vn[1], q, sizeof(T) * b->nsum, cudaMemcpyDefault, s));
+  int rc = run_batch_kernel(b, kModeUpdateVec);
+  if (rc) return rc;
+  return cudaStreamSynchronize(s) == cudaSuccess ? 0 : OSQP_ALGEBRA_LOAD_ERROR;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_solve(OSQPBatch* b) {
+  if (!b) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  cudaSetDevice(b->device);
+  cudaEventRecord(b->ev0, b->stream);
+  int rc = run_batch_kernel(b, kModeSolve);
+  if (rc) return rc;
+  cudaEventRecord(b->ev1, b->stream);
+  k_batch_info<<<(b->count + 255) / 256, 256, 0, b->stream>>>(b->B.st, b->count, b->d_info, b->d_totals);
+  long long tot[2] = {0, 0};
+  BT_TRY(cudaMemcpyAsync(tot, b->d_totals, sizeof(tot), cudaMemcpyDeviceToHost, b->stream));
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return OSQP_ALGEBRA_LOAD_ERROR;
+  cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+  b->last_admm = tot[0]; b->last_pcg = tot[1];
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_get_solution(OSQPBatch* b, OSQPFloat* x, OSQPFloat* y, OSQPInt* status,
+                                                 OSQPInt* iter, OSQPFloat* obj_val, OSQPFloat* prim_res,
+                                                 OSQPFloat* dual_res) {
+  if (!b) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  cudaStream_t s = b->stream;
+  if (x) BT_TRY(cudaMemcpyAsync(x, b->B.vn[14], sizeof(T) * b->nsum, cudaMemcpyDefault, s));
+  if (y && b->msum) BT_TRY(cudaMemcpyAsync(y, b->B.vm[12], sizeof(T) * b->msum, cudaMemcpyDefault, s));
+  if (status || iter || obj_val || prim_res || dual_res) {
+    std::vector<BatchInfo> info(b->count);
+    BT_TRY(cudaMemcpyAsync(info.data(), b->d_info, sizeof(BatchInfo) * b->count, cudaMemcpyDeviceToHost, s));
+    BT_TRY(cudaStreamSynchronize(s));
+    for (int k = 0; k < b->count; k++) {
+      if (status) status[k] = info[k].status;
+      if (iter) iter[k] = info[k].iter;
+      if (obj_val) obj_val[k] = (OSQPFloat)info[k].obj;
+      if (prim_res) prim_res[k] = (OSQPFloat)info[k].prim;
+      if (dual_res) dual_res[k] = (OSQPFloat)info[k].dual;
+    }
+  }
+  return cudaStreamSynchronize(s) == cudaSuccess ? 0 : OSQP_ALGEBRA_LOAD_ERROR;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_stats(OSQPBatch* b, double* kernel_ms, long long* admm_iter, long long* pcg_iter) {
+  if (!b) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  if (kernel_ms) *kernel_ms = b->last_ms;
+  if (admm_iter) *admm_iter = b->last_admm;
+  if (pcg_iter) *pcg_iter = b->last_pcg;
+  return 0;
+}

@@ -1,0 +1,859 @@
+// gb_solver.cuh -- the OSQP algorithm as group-generic device code.
+//
+// One OSQP problem is solved by a "group" (gb_common.cuh): a CTA for batched
+// or small problems, a cooperative persistent grid for a large one.  All
+// phases -- Ruiz scaling, rho vector, Jacobi preconditioner, ADMM iterations
+// with the reduced-KKT PCG, residual/termination evaluation, adaptive rho and
+// the solution store -- run inside one kernel launch; the only host traffic is
+// the launch and the final copy of the results.
+//
+// Reference behaviour restated here (file:line in the OSQP 1.0 sources):
+//   scaling          src/scaling.c:48-164
+//   rho vector       src/auxil.c:76-122, osqp_api.c:1412-1464
+//   ADMM steps       src/auxil.c:136-229
+//   reduced KKT PCG  algebra/cuda/lin_sys/indirect/cuda_pcg.cu:50-208,
+//                    cuda_pcg_interface.cu:32-92,229-273
+//   Jacobi           algebra/cuda/lin_sys/indirect/cuda_pcg.cu:211-285
+//   update_info      src/auxil.c:231-458,676-762
+//   termination      src/auxil.c:460-588,808-945
+//   adaptive rho     src/auxil.c:14-74; osqp_api.c:776-889
+//   solve loop       src/osqp_api.c:636-1038
+//   store_solution   src/auxil.c:598-674
+#pragma once
+
+#include <type_traits>
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+// Status values (include/public/osqp_api_constants.h:28-40)
+enum : int {
+  ST_SOLVED = 1, ST_SOLVED_INACCURATE, ST_PRIMAL_INFEASIBLE, ST_PRIMAL_INFEASIBLE_INACCURATE,
+  ST_DUAL_INFEASIBLE, ST_DUAL_INFEASIBLE_INACCURATE, ST_MAX_ITER_REACHED, ST_TIME_LIMIT_REACHED,
+  ST_NON_CVX, ST_SIGINT, ST_UNSOLVED
+};
+
+constexpr double kRhoMin = 1e-06, kRhoMax = 1e06, kRhoTol = 1e-04, kRhoEqOverIneq = 1e03;
+constexpr double kMinScaling = 1e-04, kMaxScaling = 1e+04;
+constexpr double kCgTolMin = 1e-7;
+
+// Solver settings as kernel-side plain values (OSQPSettings fields).
+struct DevSettings {
+  double rho, sigma, alpha;
+  double eps_abs, eps_rel, eps_prim_inf, eps_dual_inf;
+  double cg_tol_fraction, adaptive_rho_tolerance, adaptive_rho_fraction;
+  double time_limit;      // seconds
+  double infty;           // OSQP_INFTY of the build
+  double zero_deadzone;   // OSQP_ZERO_DEADZONE of the build
+  int scaling, rho_is_vec, max_iter, check_termination;
+  int adaptive_rho, adaptive_rho_interval;
+  int cg_max_iter, cg_tol_reduction, cg_precond;
+  int scaled_termination, check_dualgap, warm_starting;
+};
+
+// Per-problem scalar state.  Lives in global memory between launches; during
+// a launch every CTA of the group keeps an identical copy in shared memory.
+struct SolverScalars {
+  double rho, rho_inv, c, cinv;
+  double scaled_prim_res, scaled_dual_res;
+  double eps_prev, reduction_factor;
+  double obj_val, dual_obj_val, prim_res, dual_res, duality_gap;
+  double rho_estimate, rel_kkt_error, primdual_int, last_rel_kkt;
+  double xtPx, qtx, SC, scaled_dual_gap;
+  // norms kept from the last update_info (termination and rho estimate)
+  double nz_s, nAx_s, nz_u, nAx_u;          // ||z||, ||Ax|| (scaled / unscaled)
+  double nq_s, nAty_s, nPx_s, nq_u, nAty_u, nPx_u;
+  double dy_norm, dy_lhs, atdy_norm;        // primal infeasibility
+  double dx_norm, dx_q, pdx_norm, recc_max; // dual infeasibility
+  double elapsed;                           // seconds since solve start
+  double rhs_norm;
+  double pcg_rTy, pcg_rnorm, pcg_eps, pcg_alpha, pcg_beta;
+  unsigned long long t_start;
+  long long pcg_iters_total;
+  int zero_pcg_iters;
+  int status, iter, rho_updates, rho_updated;
+  int err;
+  int cancel;
+  int p_parity;
+};
+
+template <typename T>
+struct DevProblem {
+  int n, m;
+  CSR<T> P;    // full symmetric P (n x n), explicit diagonal
+  CSR<T> A;    // A (m x n)
+  CSR<T> At;   // A' (n x m) = CSC arrays of A
+  const int* Pdiag;       // position of P(i,i) in P.val
+  const int* Psrc;        // P.val[k] = Praw[Psrc[k]] (or 0 if Psrc[k] < 0)
+  const int* Asrc;        // A.val[k] = Araw[Asrc[k]]
+  const T* Praw;          // upper-triangular CSC values as given
+  const T* Araw;          // CSC values of A as given
+  T *q, *l, *u;           // scaled problem vectors
+  const T *q_in, *l_in, *u_in;  // unscaled inputs (setup only)
+  T *D, *Dinv, *E, *Einv;
+  T *rho_vec, *rho_inv_vec;
+  int* ctype;
+  T *x, *z, *y, *dx, *dy;
+  T *xp, *r, *p0, *p1, *Kp, *yv, *rhs, *t, *Minv;
+  T *xo, *yo, *pcert, *dcert;   // stored solution (unscaled)
+  T *Dt, *Et;                   // scaling scratch
+  SolverScalars* st;            // persistent scalars
+};
+
+template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
+template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
+__device__ __forceinline__ double dlimit_scaling(double v) {
+  v = v < kMinScaling ? 1.0 : v;
+  return v > kMaxScaling ? kMaxScaling : v;
+}
+template <typename T> __device__ __forceinline__ T tnan() { return T(NAN); }
+
+// P and A' share the row index space 0..n-1; one sub-warp handles row i of
+// both so the reduced-KKT product needs a single pass.
+template <int L, typename T, typename G, typename XP, typename XA, typename FN>
+__device__ __forceinline__ void kkt_rows_L(G& g, const CSR<T>& P, const CSR<T>& At, XP xp, XA xa, FN fn) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / L, sl = lane % L;
+  constexpr int RPW = 32 / L;
+  const int nw = g.nwarps(), w = g.warp();
+  const int n = P.rows;
+  for (int base = w * RPW; base < n; base += nw * RPW) {
+    const int i = base + sub;
+    T a1 = T(0), a2 = T(0);
+    if (i < n) {
+      int b = P.rowptr[i], e = P.rowptr[i + 1];
+      for (int k = b + sl; k < e; k += L) a1 += P.val[k] * xp(P.col[k]);
+      b = At.rowptr[i]; e = At.rowptr[i + 1];
+      for (int k = b + sl; k < e; k += L) a2 += At.val[k] * xa(At.col[k]);
+    }
+    a1 = subwarp_sum<L>(a1);
+    a2 = subwarp_sum<L>(a2);
+    if (i < n && sl == 0) fn(i, a1, a2);
+  }
+}
+template <typename T, typename G, typename XP, typename XA, typename FN>
+__device__ __forceinline__ void kkt_rows(G& g, int L, const CSR<T>& P, const CSR<T>& At, XP xp, XA xa, FN fn) {
+  switch (L) {
+    case 1:  kkt_rows_L<1>(g, P, At, xp, xa, fn); break;
+    case 2:  kkt_rows_L<2>(g, P, At, xp, xa, fn); break;
+    case 4:  kkt_rows_L<4>(g, P, At, xp, xa, fn); break;
+    case 8:  kkt_rows_L<8>(g, P, At, xp, xa, fn); break;
+    case 16: kkt_rows_L<16>(g, P, At, xp, xa, fn); break;
+    default: kkt_rows_L<32>(g, P, At, xp, xa, fn); break;
+  }
+}
+
+template <typename T>
+struct Solver {
+  DevProblem<T> pr;
+  DevSettings s;
+  SolverScalars* sc;  // shared-memory copy
+  int kktL;           // lanes per row for the P / A' pair
+
+  __device__ bool unscaled_term() const { return s.scaling && !s.scaled_termination; }
+  __device__ double rho_of(int j) const { return s.rho_is_vec ? (double)pr.rho_vec[j] : sc->rho; }
+
+  // ---------------------------------------------------------------------
+  // Setup: data from the raw inputs, Ruiz scaling, rho, preconditioner.
+  // ---------------------------------------------------------------------
+  template <typename G>
+  __device__ bool load_values(G& g) {
+    // row pointers hold absolute positions (a QP of a batch is a slice)
+    for_range(g, pr.P.rowptr[0], pr.P.rowptr[pr.n], [&](int k) { int s0 = pr.Psrc[k]; pr.P.val[k] = s0 >= 0 ? pr.Praw[s0] : T(0); });
+    if (pr.m) for_range(g, pr.A.rowptr[0], pr.A.rowptr[pr.m], [&](int k) { pr.A.val[k] = pr.Araw[pr.Asrc[k]]; });
+    for_range(g, pr.At.rowptr[0], pr.At.rowptr[pr.n], [&](int k) { pr.At.val[k] = pr.Araw[k]; });
+    for_each(g, pr.n, [&](int i) { pr.q[i] = pr.q_in[i]; pr.D[i] = T(1); pr.Dinv[i] = T(1); });
+    for_each(g, pr.m, [&](int j) { pr.l[j] = pr.l_in[j]; pr.u[j] = pr.u_in[j]; pr.E[j] = T(1); pr.Einv[j] = T(1); });
+    return g.sync();
+  }
+
+  template <typename G>
+  __device__ bool scale_data(G& g) {
+    const int n = pr.n, m = pr.m;
+    if (threadIdx.x == 0) sc->c = 1.0;
+    for (int pass = 0; pass < s.scaling; pass++) {
+      // column inf-norms of [P; A] (rows of symmetric P and of A') and row
+      // inf-norms of A, limited, square-rooted and inverted (scaling.c:84-101)
+      rows_norm_pair(g);
+      for_each(g, m, [&](int j) {
+        T a = T(0);
+        for (int k = pr.A.rowptr[j]; k < pr.A.rowptr[j + 1]; k++) a = tmax(a, (T)fabs((double)pr.A.val[k]));
+        pr.Et[j] = T(1) / (T)sqrt((double)(T)dlimit_scaling((double)a));
+      });
+      if (!g.sync()) return false;
+      // P <- D P D ; A <- E A D ; A' likewise ; q <- D q (scaling.c:103-117)
+      for_each_row_entries(g);
+      for_each(g, n, [&](int i) { pr.q[i] *= pr.Dt[i]; pr.D[i] *= pr.Dt[i]; });
+      for_each(g, m, [&](int j) { pr.E[j] *= pr.Et[j]; });
+      if (!g.sync()) return false;
+      // cost scaling (scaling.c:119-146)
+      Acc<T> sm[1];
+      T mx[1] = {T(0)};
+      for_each(g, n, [&](int i) {
+        T a = T(0);
+        for (int k = pr.P.rowptr[i]; k < pr.P.rowptr[i + 1]; k++) a = tmax(a, (T)fabs(pr.P.val[k]));
+        sm[0].add(a);
+        mx[0] = tmax(mx[0], (T)fabs(pr.q[i]));
+      });
+      double rs[1], rm[1];
+      g.reduce(sm, mx, rs, rm);
+      if (!g.ok()) return false;
+      double ct = rs[0] / n;
+      double nq = dlimit_scaling(rm[0]);
+      ct = dlimit_scaling(fmax(ct, nq));
+      ct = 1.0 / ct;
+      const T ctt = (T)ct;
+      for_range(g, pr.P.rowptr[0], pr.P.rowptr[n], [&](int k) { pr.P.val[k] *= ctt; });
+      for_each(g, n, [&](int i) { pr.q[i] *= ctt; });
+      if (threadIdx.x == 0) sc->c *= ct;
+      if (!g.sync()) return false;
+    }
+    if (threadIdx.x == 0) sc->cinv = 1.0 / sc->c;
+    for_each(g, n, [&](int i) { pr.Dinv[i] = T(1) / pr.D[i]; });
+    for_each(g, m, [&](int j) {
+      pr.Einv[j] = T(1) / pr.E[j];
+      pr.l[j] *= pr.E[j];
+      pr.u[j] *= pr.E[j];
+    });
+    return g.sync();
+  }
+
+  // Column norms of [P; A] for rows i (P symmetric, A' rows): Dt[i]
+  template <typename G>
+  __device__ void rows_norm_pair(G& g) {
+    for_each(g, pr.n, [&](int i) {
+      T a = T(0);
+      for (int k = pr.P.rowptr[i]; k < pr.P.rowptr[i + 1]; k++) a = tmax(a, (T)fabs((double)pr.P.val[k]));
+      T b = T(0);
+      for (int k = pr.At.rowptr[i]; k < pr.At.rowptr[i + 1]; k++) b = tmax(b, (T)fabs((double)pr.At.val[k]));
+      a = tmax(a, b);
+      pr.Dt[i] = T(1) / (T)sqrt((double)(T)dlimit_scaling((double)a));
+    });
+  }
+
+  template <typename G>
+  __device__ void for_each_row_entries(G& g) {
+    for_each(g, pr.n, [&](int i) {
+      const T di = pr.Dt[i];
+      // D_i * D_j is commutative, so the stored full P stays exactly symmetric
+      for (int k = pr.P.rowptr[i]; k < pr.P.rowptr[i + 1]; k++) pr.P.val[k] = pr.P.val[k] * (di * pr.Dt[pr.P.col[k]]);
+      for (int k = pr.At.rowptr[i]; k < pr.At.rowptr[i + 1]; k++) pr.At.val[k] = (pr.At.val[k] * pr.Et[pr.At.col[k]]) * di;
+    });
+    for_each(g, pr.m, [&](int j) {
+      const T ej = pr.Et[j];
+      for (int k = pr.A.rowptr[j]; k < pr.A.rowptr[j + 1]; k++) pr.A.val[k] = (pr.A.val[k] * ej) * pr.Dt[pr.A.col[k]];
+    });
+  }
+
+  // rho vector from constraint types (auxil.c:76-104)
+  template <typename G>
+  __device__ void set_rho_vec(G& g) {
+    const double infval = s.infty * kMinScaling;
+    const double rho = sc->rho;
+    for_each(g, pr.m, [&](int j) {
+      const double l = pr.l[j], u = pr.u[j];
+      int t;
+      if (l < -infval && u > infval) t = -1;
+      else if (u - l < kRhoTol) t = 1;
+      else t = 0;
+      pr.ctype[j] = t;
+      const double rv = t < 0 ? kRhoMin : (t == 0 ? rho : kRhoEqOverIneq * rho);
+      pr.rho_vec[j] = (T)rv;
+      pr.rho_inv_vec[j] = T(1) / (T)rv;
+    });
+  }
+  template <typename G>
+  __device__ void refresh_rho_vec(G& g) {
+    const double rho = sc->rho;
+    for_each(g, pr.m, [&](int j) {
+      const int t = pr.ctype[j];
+      const double rv = t < 0 ? kRhoMin : (t == 0 ? rho : kRhoEqOverIneq * rho);
+      pr.rho_vec[j] = (T)rv;
+      pr.rho_inv_vec[j] = T(1) / (T)rv;
+    });
+  }
+
+  // Jacobi preconditioner M = sigma + diag(P) + diag(A' R A) (cuda_pcg.cu:211-266)
+  template <typename G>
+  __device__ void update_precond(G& g) {
+    const T sig = (T)s.sigma;
+    const bool vec = s.rho_is_vec;
+    const T rho = (T)sc->rho;
+    for_each(g, pr.n, [&](int i) {
+      if (s.cg_precond == 0) { pr.Minv[i] = T(1); return; }
+      T d = T(0);
+      for (int k = pr.At.rowptr[i]; k < pr.At.rowptr[i + 1]; k++) {
+        const T a = pr.At.val[k];
+        d += vec ? a * a * pr.rho_vec[pr.At.col[k]] : a * a;
+      }
+      if (!vec) d *= rho;
+      pr.Minv[i] = T(1) / (sig + pr.P.val[pr.Pdiag[i]] + d);
+    });
+  }
+
+  template <typename G>
+  __device__ void cold_start(G& g) {
+    for_each(g, pr.n, [&](int i) { pr.x[i] = T(0); pr.xp[i] = T(0); });
+    for_each(g, pr.m, [&](int j) { pr.z[j] = T(0); pr.y[j] = T(0); });
+  }
+
+  // Values, scaling, rho vector and preconditioner.  keep = true is the matrix
+  // update path (osqp_api.c:1309-1409): rho and the iterates are kept.
+  template <typename G>
+  __device__ bool prepare_data(G& g, bool keep) {
+    if (!load_values(g)) return false;
+    if (s.scaling) { if (!scale_data(g)) return false; }
+    else if (threadIdx.x == 0) { sc->c = 1.0; sc->cinv = 1.0; }
+    if (!keep && s.rho_is_vec) set_rho_vec(g);
+    if (!g.sync()) return false;
+    update_precond(g);
+    return g.sync();
+  }
+
+  // Whole setup: values, scaling, rho, preconditioner, cold start.
+  template <typename G>
+  __device__ bool setup(G& g) {
+    if (threadIdx.x == 0) {
+      sc->c = 1.0; sc->cinv = 1.0;
+      sc->rho = fmin(fmax(s.rho, kRhoMin), kRhoMax);
+      sc->rho_inv = 1.0 / sc->rho;
+      sc->rho_updates = 0; sc->status = ST_UNSOLVED; sc->iter = 0;
+      sc->scaled_prim_res = 0.0; sc->scaled_dual_res = 0.0;
+      sc->obj_val = s.infty; sc->prim_res = s.infty; sc->dual_res = s.infty;
+      sc->rel_kkt_error = s.infty; sc->last_rel_kkt = s.infty;
+      sc->rho_estimate = sc->rho; sc->primdual_int = 0.0;
+      sc->zero_pcg_iters = 0; sc->reduction_factor = s.cg_tol_fraction; sc->eps_prev = 1.0;
+      sc->err = 0; sc->p_parity = 0; sc->pcg_iters_total = 0; sc->cancel = 0;
+    }
+    __syncthreads();
+    if (!prepare_data(g, false)) return false;
+    cold_start(g);
+    return g.sync();
+  }
+
+  // ---------------------------------------------------------------------
+  // One ADMM iteration (auxil.c:136-229) with the PCG solve in between.
+  // ---------------------------------------------------------------------
+  template <typename G>
+  __device__ bool admm_iteration(G& g, int iter) {
+    const int n = pr.n, m = pr.m;
+    const bool vec = s.rho_is_vec;
+    const T sig = (T)s.sigma;
+    const T rho_s = (T)sc->rho, rinv_s = (T)sc->rho_inv;
+    T* __restrict__ x = pr.x; T* __restrict__ z = pr.z; T* __restrict__ y = pr.y;
+    T* __restrict__ xp = pr.xp;
+
+    // Phase R: rhs = (sigma x - q) + A'(rho .* (z - rho^-1 y)) and t = rho .* (A xp)
+    Acc<T> sm0[1];
+    T mx0[3] = {T(0), T(-INFINITY), T(-INFINITY)};
+    rows_apply(g, pr.At,
+      [&](int j) {
+        const T rj = vec ? pr.rho_vec[j] : rho_s;
+        const T ij = vec ? pr.rho_inv_vec[j] : rinv_s;
+        return rj * (z[j] - ij * y[j]);
+      },
+      [&](int i, T v) {
+        const T b1 = sig * x[i] - pr.q[i];
+        const T rr = b1 + v;
+        pr.rhs[i] = rr;
+        mx0[0] = tmax(mx0[0], (T)fabs(rr));
+      });
+    if (m > 0) {
+      rows_apply(g, pr.A, [&](int c) { return xp[c]; },
+        [&](int j, T v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
+    }
+    // time / cancellation ride on this reduction so every CTA sees the same values
+    if (g.tid() == 0) {
+      mx0[1] = (T)((double)(global_ns() - sc->t_start) * 1e-9);
+      mx0[2] = (T)(*((volatile int*)&pr.st->cancel));
+    }
+    double rs0[1], rm0[3];
+    g.reduce(sm0, mx0, rs0, rm0);
+    if (!g.ok()) return false;
+    const double rhs_norm = rm0[0];
+    const double elapsed = rm0[1];
+    const int cancel = rm0[2] > 0.0;
+
+    // PCG tolerance (cuda_pcg_interface.cu:32-64), computed once per CTA
+    if (threadIdx.x == 0) {
+      double e;
+      if (iter == 1) {
+        sc->reduction_factor = s.cg_tol_fraction;
+        sc->eps_prev = rhs_norm < kCgTolMin ? 1.0 : rhs_norm * sc->reduction_factor;
+        e = sc->eps_prev;
+      } else {
+        if (sc->zero_pcg_iters >= s.cg_tol_reduction) {
+          sc->reduction_factor /= 2;
+          sc->zero_pcg_iters = 0;
+        }
+        e = sc->reduction_factor * sqrt(sc->scaled_prim_res * sc->scaled_dual_res);
+        e = fmax(fmin(e, sc->eps_prev), kCgTolMin);
+        sc->eps_prev = e;
+      }
+      sc->pcg_eps = e;
+      sc->rhs_norm = rhs_norm;
+    }
+    __syncthreads();
+    const double eps = sc->pcg_eps;
+
+    // Phase I: r = K xp - rhs, yv = M^-1 r, p = -yv, rTy, ||r||
+    T* pA = sc->p_parity ? pr.p1 : pr.p0;
+    Acc<T> sm1[1];
+    T mx1[1] = {T(0)};
+    kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return xp[c]; }, [&](int c) { return m ? pr.t[c] : T(0); },
+      [&](int i, T pv, T av) {
+        const T kx = sig * xp[i] + pv + av;
+        const T r = kx - pr.rhs[i];
+        const T yv = pr.Minv[i] * r;
+        pr.r[i] = r; pr.yv[i] = yv; pA[i] = -yv;
+        sm1[0].add_prod(yv, r);
+        mx1[0] = tmax(mx1[0], (T)fabs(r));
+      });
+    double rs1[1], rm1[1];
+    g.reduce(sm1, mx1, rs1, rm1);
+    if (!g.ok()) return false;
+    double rTy = rs1[0], rnorm = rm1[0];
+
+    // PCG loop (cuda_pcg.cu:155-200).  Four phases per iteration; each ends
+    // at a group barrier (the two reductions carry theirs).
+    T* p = pA;
+    int it = 0;
+    while (rnorm > eps && it < s.cg_max_iter) {
+      // Phase A: t = rho .* (A p)
+      if (m > 0) {
+        rows_apply(g, pr.A, [&](int c) { return p[c]; },
+                   [&](int j, T v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
+        if (!g.sync()) return false;
+      }
+      // Phase B: Kp = sigma p + P p + A' t ; pKp
+      Acc<T> sm2[1];
+      T mx2[1] = {T(0)};
+      kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return p[c]; }, [&](int c) { return m ? pr.t[c] : T(0); },
+        [&](int i, T pv, T av) {
+          const T pi = p[i];
+          const T kp = sig * pi + pv + av;
+          pr.Kp[i] = kp;
+          sm2[0].add_prod(pi, kp);
+        });
+      double rs2[1], rm2[1];
+      g.reduce(sm2, mx2, rs2, rm2);
+      if (!g.ok()) return false;
+      const double alpha = rTy / rs2[0];
+      const T at = (T)alpha;
+      // Phase C: x += alpha p ; r += alpha Kp ; yv = M^-1 r ; rTy ; ||r||
+      Acc<T> sm3[1];
+      T mx3[1] = {T(0)};
+      for_each(g, n, [&](int i) {
+        xp[i] += at * p[i];
+        const T r = pr.r[i] + at * pr.Kp[i];
+        pr.r[i] = r;
+        const T yv = pr.Minv[i] * r;
+        pr.yv[i] = yv;
+        sm3[0].add_prod(yv, r);
+        mx3[0] = tmax(mx3[0], (T)fabs(r));
+      });
+      double rs3[1], rm3[1];
+      g.reduce(sm3, mx3, rs3, rm3);
+      if (!g.ok()) return false;
+      const double rTy_new = rs3[0];
+      const double beta = rTy_new / rTy;
+      rTy = rTy_new;
+      rnorm = rm3[0];
+      it++;
+      // Phase D: p = beta p - yv (skipped when the loop is about to end)
+      if (rnorm > eps && it < s.cg_max_iter) {
+        const T bt = (T)beta;
+        for_each(g, n, [&](int i) { p[i] = bt * p[i] - pr.yv[i]; });
+        if (!g.sync()) return false;
+      }
+    }
+    if (threadIdx.x == 0) {
+      sc->pcg_iters_total += it;
+      if (it == 0) sc->zero_pcg_iters++; else sc->zero_pcg_iters = 0;
+      sc->elapsed = elapsed;
+      sc->cancel = cancel;
+    }
+
+    // Phase U: x~ = xp, z~ = A xp, then the x / z / y updates (auxil.c:172-229)
+    const T al = (T)s.alpha, oma = (T)(1.0 - s.alpha);
+    for_each(g, n, [&](int i) {
+      const T xo = x[i];
+      const T xn = al * xp[i] + oma * xo;
+      x[i] = xn;
+      pr.dx[i] = xn - xo;
+    });
+    if (m > 0) {
+      rows_apply(g, pr.A, [&](int c) { return xp[c]; }, [&](int j, T zt) {
+        const T ri = vec ? pr.rho_inv_vec[j] : rinv_s;
+        const T rr = vec ? pr.rho_vec[j] : rho_s;
+        const T zo = z[j];
+        const T zr = al * zt + oma * zo;
+        const T zz = zr + ri * y[j];
+        const T zn = tmin(tmax(zz, pr.l[j]), pr.u[j]);
+        const T d = rr * (zr - zn);
+        z[j] = zn;
+        pr.dy[j] = d;
+        y[j] = y[j] + d;
+      });
+    }
+    __syncthreads();
+    return g.sync();
+  }
+
+  // ---------------------------------------------------------------------
+  // Residuals, objective and all termination quantities (update_info).
+  // ---------------------------------------------------------------------
+  template <typename G>
+  __device__ bool update_info(G& g, int iter) {
+    const int n = pr.n, m = pr.m;
+    const double infval = s.infty * kMinScaling;
+    const bool uns = unscaled_term();
+    T* x = pr.x; T* z = pr.z; T* y = pr.y;
+
+    // Phase T1 over the rows of A: Ax, A dx and the m-length terms.
+    // mx: 0 |Ax-z|  1 |Einv(Ax-z)|  2 |z|  3 |Ax|  4 |Einv z|  5 |Einv Ax|
+    //     6 |dy_proj|  7 |E dy_proj|  8 recession-cone violation of (Einv) A dx
+    // sm: 0 support function  1 u'max(dy,0) + l'min(dy,0)
+    Acc<T> sm[2];
+    T mx[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) mx[k] = (k == 8) ? T(-INFINITY) : T(0);
+    if (m > 0) {
+      rows_apply2(g, pr.A, [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; },
+        [&](int j, T ax, T adx) {
+          const T l = pr.l[j], u = pr.u[j];
+          const T ei = pr.Einv[j];
+          const T zj = z[j];
+          const T pres = ax - zj;
+          mx[0] = tmax(mx[0], (T)fabs(pres));
+          mx[1] = tmax(mx[1], (T)fabs(ei * pres));
+          mx[2] = tmax(mx[2], (T)fabs(zj));
+          mx[3] = tmax(mx[3], (T)fabs(ax));
+          mx[4] = tmax(mx[4], (T)fabs(ei * zj));
+          mx[5] = tmax(mx[5], (T)fabs(ei * ax));
+          // support function of [l,u] at y (auxil.c:254-266)
+          T yp = y[j];
+          if ((double)u > infval) yp = ((double)l < -infval) ? T(0) : tmin(yp, T(0));
+          else if ((double)l < -infval) yp = tmax(yp, T(0));
+          if (fabs((double)yp) < s.zero_deadzone) yp = T(0);
+          sm[0].add_prod(u, tmax(yp, T(0)));
+          sm[0].add_prod(l, tmin(yp, T(0)));
+          // project dy onto the polar recession cone (in place) (auxil.c:476-480)
+          T dp = pr.dy[j];
+          if ((double)u > infval) dp = ((double)l < -infval) ? T(0) : tmin(dp, T(0));
+          else if ((double)l < -infval) dp = tmax(dp, T(0));
+          pr.dy[j] = dp;
+          mx[6] = tmax(mx[6], (T)fabs(dp));
+          mx[7] = tmax(mx[7], (T)fabs(pr.E[j] * dp));
+          sm[1].add_prod(u, tmax(dp, T(0)));
+          sm[1].add_prod(l, tmin(dp, T(0)));
+          // recession cone test of A dx (vector.c:704-727): violation if
+          // (u finite and v > tol) or (l finite and v < -tol)
+          const T v = uns ? adx * ei : adx;
+          T viol = T(-INFINITY);
+          if ((double)u < infval) viol = tmax(viol, v);
+          if ((double)l > -infval) viol = tmax(viol, -v);
+          mx[8] = tmax(mx[8], viol);
+        });
+    }
+    double smr[2], mxr[9];
+    g.reduce(sm, mx, smr, mxr);
+    if (!g.ok()) return false;
+
+    // Phase T2 over the rows of P / A': Px, P dx, A'y, A'dy and the n-length terms.
+    // mx: 0 |q+Px+A'y|  1 |Dinv(q+Px+A'y)|  2 |q|  3 |A'y|  4 |Px|  5 |Dinv q|
+    //     6 |Dinv A'y|  7 |Dinv Px|  8 |dx|  9 |D dx|  10 |P dx|  11 |Dinv P dx|
+    //     12 |A'dy|  13 |Dinv A'dy|
+    // sm: 0 x'Px  1 q'x  2 q'dx
+    Acc<T> s2[3];
+    T m2[14];
+#pragma unroll
+    for (int k = 0; k < 14; k++) m2[k] = T(0);
+    {
+      const int L = kktL;
+      auto body = [&](auto Lc) {
+        constexpr int LL = decltype(Lc)::value;
+        const int lane = threadIdx.x & 31;
+        const int sub = lane / LL, sl = lane % LL;
+        constexpr int RPW = 32 / LL;
+        const int nw = g.nwarps(), w = g.warp();
+        for (int base = w * RPW; base < n; base += nw * RPW) {
+          const int i = base + sub;
+          T px = T(0), pdx = T(0), aty = T(0), atdy = T(0);
+          if (i < n) {
+            int b = pr.P.rowptr[i], e = pr.P.rowptr[i + 1];
+            for (int k = b + sl; k < e; k += LL) {
+              const T v = pr.P.val[k]; const int c = pr.P.col[k];
+              px += v * x[c]; pdx += v * pr.dx[c];
+            }
+            b = pr.At.rowptr[i]; e = pr.At.rowptr[i + 1];
+            for (int k = b + sl; k < e; k += LL) {
+              const T v = pr.At.val[k]; const int c = pr.At.col[k];
+              aty += v * y[c]; atdy += v * pr.dy[c];
+            }
+          }
+          px = subwarp_sum<LL>(px); pdx = subwarp_sum<LL>(pdx);
+          aty = subwarp_sum<LL>(aty); atdy = subwarp_sum<LL>(atdy);
+          if (i < n && sl == 0) {
+            const T q = pr.q[i];
+            const T di = pr.Dinv[i];
+            const T dr = (m > 0) ? (q + px) + aty : q + px;
+            m2[0] = tmax(m2[0], (T)fabs(dr));
+            m2[1] = tmax(m2[1], (T)fabs(di * dr));
+            m2[2] = tmax(m2[2], (T)fabs(q));
+            m2[3] = tmax(m2[3], (T)fabs(aty));
+            m2[4] = tmax(m2[4], (T)fabs(px));
+            m2[5] = tmax(m2[5], (T)fabs(di * q));
+            m2[6] = tmax(m2[6], (T)fabs(di * aty));
+            m2[7] = tmax(m2[7], (T)fabs(di * px));
+            const T dxi = pr.dx[i];
+            m2[8] = tmax(m2[8], (T)fabs(dxi));
+            m2[9] = tmax(m2[9], (T)fabs(pr.D[i] * dxi));
+            m2[10] = tmax(m2[10], (T)fabs(pdx));
+            m2[11] = tmax(m2[11], (T)fabs(pdx * di));
+            m2[12] = tmax(m2[12], (T)fabs(atdy));
+            m2[13] = tmax(m2[13], (T)fabs(atdy * di));
+            s2[0].add_prod(px, x[i]);
+            s2[1].add_prod(q, x[i]);
+            s2[2].add_prod(q, dxi);
+          }
+        }
+      };
+      switch (L) {
+        case 1:  body(std::integral_constant<int, 1>{}); break;
+        case 2:  body(std::integral_constant<int, 2>{}); break;
+        case 4:  body(std::integral_constant<int, 4>{}); break;
+        case 8:  body(std::integral_constant<int, 8>{}); break;
+        case 16: body(std::integral_constant<int, 16>{}); break;
+        default: body(std::integral_constant<int, 32>{}); break;
+      }
+    }
+    double s2r[3], m2r[14];
+    g.reduce(s2, m2, s2r, m2r);
+    if (!g.ok()) return false;
+
+    if (threadIdx.x == 0) {
+      SolverScalars* c = sc;
+      // primal residual (auxil.c:308-332)
+      double prim = 0.0;
+      if (m > 0) {
+        c->scaled_prim_res = mxr[0];
+        prim = uns ? mxr[1] : mxr[0];
+      }
+      // dual residual (auxil.c:371-407)
+      c->scaled_dual_res = m2r[0];
+      const double dual = uns ? c->cinv * m2r[1] : m2r[0];
+      // objective and gap (auxil.c:231-285)
+      const double quad = s2r[0], lin = s2r[1], sup = smr[0];
+      double po = 0.5 * quad + lin, dob = -0.5 * quad - sup, gap;
+      c->scaled_dual_gap = quad + lin + sup;
+      if (s.scaling) { po *= c->cinv; dob *= c->cinv; gap = c->cinv * c->scaled_dual_gap; }
+      else gap = c->scaled_dual_gap;
+      c->xtPx = quad; c->qtx = lin; c->SC = sup;
+      c->obj_val = po; c->dual_obj_val = dob; c->duality_gap = gap;
+      c->prim_res = prim; c->dual_res = dual;
+      c->iter = iter;
+      c->primdual_int += fabs(gap);
+      c->rel_kkt_error = fmax(fmax(dual, prim), gap);
+      // norms for tolerances and the rho estimate
+      c->nz_s = mxr[2]; c->nAx_s = mxr[3]; c->nz_u = mxr[4]; c->nAx_u = mxr[5];
+      c->nq_s = m2r[2]; c->nAty_s = m2r[3]; c->nPx_s = m2r[4];
+      c->nq_u = m2r[5]; c->nAty_u = m2r[6]; c->nPx_u = m2r[7];
+      // infeasibility quantities
+      c->dy_norm = uns ? mxr[7] : mxr[6];
+      c->dy_lhs = smr[1];
+      c->atdy_norm = uns ? m2r[13] : m2r[12];
+      c->dx_norm = uns ? m2r[9] : m2r[8];
+      c->dx_q = s2r[2];
+      c->pdx_norm = uns ? m2r[11] : m2r[10];
+      c->recc_max = mxr[8];
+    }
+    __syncthreads();
+    return true;
+  }
+
+  // check_termination (auxil.c:808-945) on the quantities from update_info.
+  // Scalar code executed by thread 0 of every CTA.
+  __device__ int check_termination_scalar(int approximate) {
+    SolverScalars* c = sc;
+    const bool uns = unscaled_term();
+    const double div_tol = 1.0 / s.infty;
+    double ea = s.eps_abs, er = s.eps_rel, epi = s.eps_prim_inf, edi = s.eps_dual_inf;
+    int prc = 0, drc = 0, pic = 0, dic = 0, gc = 0;
+    if (c->prim_res > s.infty || c->dual_res > s.infty) {
+      c->status = ST_NON_CVX;
+      c->obj_val = NAN;
+      return 1;
+    }
+    if (approximate) { ea *= 10; er *= 10; epi *= 10; edi *= 10; }
+    if (pr.m == 0) prc = 1;
+    else {
+      const double base = uns ? fmax(c->nz_u, c->nAx_u) : fmax(c->nz_s, c->nAx_s);
+      if (c->prim_res < ea + er * base) prc = 1;
+      else if (c->dy_norm > div_tol && c->dy_lhs < 0.0)
+        pic = c->atdy_norm < epi * c->dy_norm;
+    }
+    double dbase = uns ? c->cinv * fmax(fmax(c->nq_u, c->nAty_u), c->nPx_u)
+                       : fmax(fmax(c->nq_s, c->nAty_s), c->nPx_s);
+    if (c->dual_res < ea + er * dbase) drc = 1;
+    else {
+      const double cs = uns ? c->c : 1.0;
+      if (c->dx_norm > div_tol && c->dx_q < 0.0 && c->pdx_norm < cs * edi * c->dx_norm)
+        dic = c->recc_max <= edi * c->dx_norm;
+    }
+    if (s.check_dualgap) {
+      double r = fmax(fmax(fabs(c->xtPx), fabs(c->qtx)), fabs(c->SC));
+      if (uns) r *= c->cinv;
+      const double g = uns ? c->duality_gap : c->scaled_dual_gap;
+      gc = fabs(g) < ea + er * r;
+    } else gc = 1;
+    if (prc && drc && gc) { c->status = approximate ? ST_SOLVED_INACCURATE : ST_SOLVED; return 1; }
+    if (pic) { c->status = approximate ? ST_PRIMAL_INFEASIBLE_INACCURATE : ST_PRIMAL_INFEASIBLE; c->obj_val = s.infty; return 1; }
+    if (dic) { c->status = approximate ? ST_DUAL_INFEASIBLE_INACCURATE : ST_DUAL_INFEASIBLE; c->obj_val = -s.infty; return 1; }
+    return 0;
+  }
+
+  // compute_rho_estimate (auxil.c:14-47)
+  __device__ double rho_estimate_scalar() const {
+    const double div_tol = 1.0 / s.infty;
+    double p = sc->scaled_prim_res / (fmax(sc->nz_s, sc->nAx_s) + div_tol);
+    double d = sc->scaled_dual_res / (fmax(fmax(sc->nq_s, sc->nAty_s), sc->nPx_s) + div_tol);
+    double r = sc->rho * sqrt(p / d);
+    return fmin(fmax(r, kRhoMin), kRhoMax);
+  }
+
+  // ---------------------------------------------------------------------
+  // The solve loop (osqp_api.c:636-1038)
+  // ---------------------------------------------------------------------
+  template <typename G>
+  __device__ bool solve(G& g) {
+    __shared__ int s_flags[4];
+    if (threadIdx.x == 0) {
+      sc->t_start = global_ns();
+      s_flags[0] = 0;
+      sc->status = ST_UNSOLVED;
+      sc->pcg_iters_total = 0;
+    }
+    if (!s.warm_starting) { cold_start(g); }
+    if (!g.sync()) return false;
+    int can_check = 0;
+    int iter;
+    for (iter = 1; iter <= s.max_iter; iter++) {
+      if (!admm_iteration(g, iter)) return false;
+      if (threadIdx.x == 0) {
+        int stop = 0;
+        if (sc->cancel) { sc->status = ST_SIGINT; stop = 2; }
+        else if (s.time_limit > 0 && sc->elapsed >= s.time_limit) { sc->status = ST_TIME_LIMIT_REACHED; stop = 1; }
+        s_flags[0] = stop;
+        int cc = s.check_termination && (iter % s.check_termination == 0);
+        int ca = 0;
+        if (s.adaptive_rho == 1 || s.adaptive_rho == 3)
+          ca = s.adaptive_rho_interval && (iter % s.adaptive_rho_interval == 0);
+        s_flags[1] = cc; s_flags[2] = ca;
+      }
+      __syncthreads();
+      if (s_flags[0]) break;
+      can_check = s_flags[1];
+      int can_adapt = s_flags[2];
+      if (can_check || can_adapt || iter == 1) { if (!update_info(g, iter)) return false; }
+      if (threadIdx.x == 0) {
+        s_flags[3] = 0;
+        if (can_check && check_termination_scalar(0)) s_flags[3] = 1;
+        sc->rho_updated = 0;
+        int ca = can_adapt;
+        if (!s_flags[3]) {
+          if (ca && s.adaptive_rho == 3) ca = sc->rel_kkt_error <= s.adaptive_rho_fraction * sc->last_rel_kkt;
+          if (ca) {
+            double rn = rho_estimate_scalar();
+            sc->rho_estimate = rn;
+            if (rn > sc->rho * s.adaptive_rho_tolerance || rn < sc->rho / s.adaptive_rho_tolerance) {
+              sc->rho = fmin(fmax(rn, kRhoMin), kRhoMax);
+              sc->rho_inv = 1.0 / sc->rho;
+              sc->rho_updates += 1;
+              sc->rho_updated = 1;
+            }
+          }
+          if (sc->rho_updated) sc->last_rel_kkt = sc->rel_kkt_error;
+        }
+      }
+      __syncthreads();
+      if (s_flags[3]) break;
+      if (sc->rho_updated) {
+        if (s.rho_is_vec) { refresh_rho_vec(g); if (!g.sync()) return false; }
+        update_precond(g);
+        if (!g.sync()) return false;
+      }
+    }
+    // post-loop (osqp_api.c:906-960); an interrupted solve skips it, as the
+    // reference jumps to its exit label on SIGINT
+    if (s_flags[0] != 2) {
+      if (!can_check) {
+        if (!update_info(g, iter - 1)) return false;
+        if (threadIdx.x == 0) check_termination_scalar(0);
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        if (sc->status == ST_UNSOLVED) {
+          if (!check_termination_scalar(1)) sc->status = ST_MAX_ITER_REACHED;
+        } else if (sc->status == ST_TIME_LIMIT_REACHED) {
+          check_termination_scalar(1);
+        }
+        sc->rho_estimate = rho_estimate_scalar();
+      }
+      __syncthreads();
+    }
+    return store_solution(g);
+  }
+
+  __host__ __device__ static bool has_solution(int st) {
+    return st != ST_PRIMAL_INFEASIBLE && st != ST_PRIMAL_INFEASIBLE_INACCURATE &&
+           st != ST_DUAL_INFEASIBLE && st != ST_DUAL_INFEASIBLE_INACCURATE && st != ST_NON_CVX;
+  }
+
+  // store_solution (auxil.c:598-674) into xo / yo / pcert / dcert
+  template <typename G>
+  __device__ bool store_solution(G& g) {
+    const int st = sc->status, n = pr.n, m = pr.m;
+    const bool uns = unscaled_term();
+    if (has_solution(st)) {
+      const T cinv = (T)sc->cinv;
+      for_each(g, n, [&](int i) {
+        pr.xo[i] = s.scaling ? pr.D[i] * pr.x[i] : pr.x[i];
+        pr.dcert[i] = tnan<T>(); pr.dx[i] = tnan<T>();
+      });
+      for_each(g, m, [&](int j) {
+        pr.yo[j] = s.scaling ? (pr.E[j] * pr.y[j]) * cinv : pr.y[j];
+        pr.pcert[j] = tnan<T>(); pr.dy[j] = tnan<T>();
+      });
+      return g.sync();
+    }
+    const bool pinf = st == ST_PRIMAL_INFEASIBLE || st == ST_PRIMAL_INFEASIBLE_INACCURATE;
+    const bool dinf = st == ST_DUAL_INFEASIBLE || st == ST_DUAL_INFEASIBLE_INACCURATE;
+    // certificates in the user's scaling (auxil.c:914-935)
+    if (pinf && uns) for_each(g, m, [&](int j) { pr.dy[j] *= pr.E[j]; });
+    if (dinf && uns) for_each(g, n, [&](int i) { pr.dx[i] *= pr.D[i]; });
+    if (!g.sync()) return false;
+    Acc<T> sm[1];
+    T mx[2] = {T(0), T(0)};
+    for_each(g, m, [&](int j) { mx[0] = tmax(mx[0], (T)fabs(pr.dy[j])); });
+    for_each(g, n, [&](int i) { mx[1] = tmax(mx[1], (T)fabs(pr.dx[i])); });
+    double smr[1], mxr[2];
+    g.reduce(sm, mx, smr, mxr);
+    if (!g.ok()) return false;
+    const T iny = (T)(1.0 / mxr[0]), inx = (T)(1.0 / mxr[1]);
+    for_each(g, n, [&](int i) {
+      pr.xo[i] = tnan<T>();
+      pr.dcert[i] = dinf ? pr.dx[i] * inx : tnan<T>();
+      pr.x[i] = T(0); pr.xp[i] = T(0);
+    });
+    for_each(g, m, [&](int j) {
+      pr.yo[j] = tnan<T>();
+      pr.pcert[j] = pinf ? pr.dy[j] * iny : tnan<T>();
+      pr.z[j] = T(0); pr.y[j] = T(0);
+    });
+    return g.sync();
+  }
+};
+
+}  // namespace gb

@@ -1,0 +1,94 @@
+"""Batched engine (osqp_gb300_batch_*): parity per QP with the FP64 oracle, and
+the same result for a QP alone and inside a mixed batch."""
+import numpy as np
+import pytest
+
+from osqp_gb300 import load
+from osqp_gb300 import problems as pb
+from osqp_gb300.api import OSQP, Batch, SOLVED, DIRECT_SOLVER, objective
+
+pytestmark = pytest.mark.gpu
+
+WORKLOAD = dict(rho=0.1, sigma=1e-6, alpha=1.6, scaling=10, eps_abs=1e-3, eps_rel=1e-3, rho_is_vec=1,
+                check_termination=5, adaptive_rho_tolerance=5.0, max_iter=4000, check_dualgap=1)
+
+
+def _mix(count, seed=0):
+    probs = []
+    for k in range(count):
+        if k % 5 == 3:
+            probs.append(pb.portfolio(seed * 1000 + k, n=120 + 7 * k))
+        elif k % 5 == 4:
+            probs.append(pb.random_qp(seed * 1000 + k, n=40 + k, m=60 + 2 * k))
+        else:
+            probs.append(pb.mpc(seed * 1000 + k))
+    return probs
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_batch_matches_oracle(prec, oracle_lib):
+    lib = load(prec)
+    probs = _mix(15, seed=1)
+    b = Batch(lib)
+    assert b.setup(probs, **WORKLOAD) == 0
+    assert b.solve() == 0
+    sol = b.solution()
+    xs = b.split(sol["x"], "n")
+    for k, d in enumerate(probs):
+        so = OSQP(oracle_lib)
+        assert so.setup(*d, linsys_solver=DIRECT_SOLVER, **WORKLOAD) == 0
+        ro = so.solve()
+        assert sol["status"][k] == ro.info["status_val"], k
+        if ro.info["status_val"] == SOLVED:
+            og = objective(d[0], d[1], xs[k].astype(np.float64))
+            oo = ro.info["obj_val"]
+            assert abs(og - oo) <= 1e-3 * max(1.0, abs(oo)), (k, og, oo)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_alone_and_in_mix_identical(prec):
+    """A QP gives bit-identical results solved alone or inside a batch."""
+    lib = load(prec)
+    probs = _mix(12, seed=2)
+    big = Batch(lib)
+    assert big.setup(probs, **WORKLOAD) == 0 and big.solve() == 0
+    sb = big.solution()
+    xs_big = big.split(sb["x"], "n")
+    for k in (0, 3, 4, 11):
+        one = Batch(lib)
+        assert one.setup([probs[k]], **WORKLOAD) == 0 and one.solve() == 0
+        s1 = one.solution()
+        assert s1["status"][0] == sb["status"][k]
+        assert s1["iter"][0] == sb["iter"][k]
+        assert np.array_equal(s1["x"], xs_big[k])
+
+
+def test_batch_update_bounds_and_resolve(oracle_lib):
+    """Receding-horizon step: new initial state -> new bounds for every QP."""
+    lib = load("f32")
+    rng = np.random.default_rng(3)
+    probs = [pb.mpc(500 + k) for k in range(8)]
+    b = Batch(lib)
+    assert b.setup(probs, **WORKLOAD) == 0 and b.solve() == 0
+    ls, us, probs2 = [], [], []
+    for (P, q, A, l, u) in probs:
+        # leading rows with a single nonzero are the initial-state equalities (-x0)
+        rowlen = np.diff(A.tocsr().indptr)
+        nx = int(np.argmax(rowlen != 1))
+        l2, u2 = pb.mpc_x0_bounds(l, u, rng.uniform(-1.0, 1.0, nx))
+        ls.append(l2); us.append(u2); probs2.append((P, q, A, l2, u2))
+    assert b.update(l=np.concatenate(ls), u=np.concatenate(us)) == 0
+    assert b.solve() == 0
+    sol = b.solution()
+    xs = b.split(sol["x"], "n")
+    for k, d in enumerate(probs2):
+        so = OSQP(oracle_lib)
+        assert so.setup(*d, linsys_solver=DIRECT_SOLVER, **WORKLOAD) == 0
+        ro = so.solve()
+        assert sol["status"][k] == ro.info["status_val"]
+        if ro.info["status_val"] == SOLVED:
+            og = objective(d[0], d[1], xs[k].astype(np.float64))
+            assert abs(og - ro.info["obj_val"]) <= 1e-3 * max(1.0, abs(ro.info["obj_val"]))
+    # invalid bounds are rejected
+    bad_l = np.concatenate(ls) + 100.0
+    assert b.update(l=bad_l, u=np.concatenate(us)) != 0
