@@ -1,0 +1,379 @@
+"""Benchmark: QP solves/s of the batched GB300 OSQP engine on batched linear MPC.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--count 4096] [--workload mpc_batch|random_qp|large_sparse]
+
+Workload (default, "mpc_batch"): 4096 seeded linear-MPC QPs of uneven size
+(horizon T~U{10..50}, nx~U{8..40}, nu~U{4..16}; stacked sparse OSQP form,
+FP32 values, int32 indices).  One step is one receding-horizon round: every
+QP receives a new initial state x0 (new l, u) and is solved from a cold start
+to eps_abs = eps_rel = 1e-3.  The QP structures are set up once, outside the
+timed region, as an MPC controller would.
+
+  value   QPs solved per second with the new bounds already in HBM (device
+          time of update + solve, CUDA events on the library's stream)
+  e2e     the same through the public C API from pinned host memory: the
+          new l, u are copied in and x plus the statuses copied out inside
+          the timed region (host wall clock around synchronous calls)
+  roofline  algorithmic bytes of the solve kernel (osqp_gb300/roofline.py)
+            over its CUDA-event time, against the measured HBM copy peak
+  cpu_baseline  the FP64 CPU oracle (OSQP's builtin algebra restated; direct
+            LDL^T KKT solver) on the machine's host cores, process pool, over a
+            bounded sample of the same QPs and steps
+
+--impl reference prints the CPU reference arm (the oracle port on all host
+cores) on the same workload.  With --gpus N > 1 (torchrun) every rank solves
+its own replica of the batch (weak scaling) and rank 0 reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+from osqp_gb300 import problems as pb  # noqa: E402
+from osqp_gb300.roofline import solve_bytes, pfull_nnz  # noqa: E402
+
+SETTINGS = dict(rho=0.1, sigma=1e-6, alpha=1.6, scaling=10, eps_abs=1e-3, eps_rel=1e-3, rho_is_vec=1,
+                check_termination=5, adaptive_rho_tolerance=5.0, max_iter=4000, check_dualgap=1,
+                warm_starting=0, polishing=0)
+
+
+def _nx_of(A):
+    rowlen = np.diff(A.tocsr().indptr)
+    return int(np.argmax(rowlen != 1))
+
+
+def make_workload(count, steps, seed=3):
+    probs = pb.mpc_batch(count, seed=seed)
+    nxs = [_nx_of(p[2]) for p in probs]
+    ls, us = [], []
+    for s in range(steps):
+        rg = np.random.default_rng([seed, 7919, s])
+        lrow, urow = [], []
+        for (P, q, A, l, u), nx in zip(probs, nxs):
+            l2, u2 = pb.mpc_x0_bounds(l, u, rg.uniform(-1.0, 1.0, nx))
+            lrow.append(l2); urow.append(u2)
+        ls.append(np.concatenate(lrow)); us.append(np.concatenate(urow))
+    return probs, ls, us
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", "bench_clocks.csv")
+
+    def start(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm_, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm_)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle arm (the reference's builtin algorithm, FP64, direct LDL^T)
+# ---------------------------------------------------------------------------
+def _cpu_worker(args):
+    lib_path, probs, lsteps, usteps = args
+    from osqp_gb300.api import Library, OSQP, DIRECT_SOLVER
+    lib = Library(lib_path, 64)
+    solvers = []
+    for (P, q, A, l, u) in probs:
+        s = OSQP(lib)
+        s.setup(P, q, A, l, u, linsys_solver=DIRECT_SOLVER, **SETTINGS)
+        solvers.append(s)
+    objs = []
+    t0 = time.perf_counter()
+    for ls, us in zip(lsteps, usteps):
+        objs = []
+        for s, l, u in zip(solvers, ls, us):
+            s.update(l=l, u=u)
+            r = s.solve()
+            objs.append((r.info["status_val"], r.info["obj_val"]))
+    return time.perf_counter() - t0, len(solvers) * len(lsteps), objs
+
+
+def cpu_arm(probs, ls, us, sizes_m, budget_s=15.0, steps=1):
+    """Oracle on all host cores: a bounded sample of QPs x steps; returns solves/s."""
+    lib_path = os.path.join(REPO, "oracle", "_build", "liboracle.so")
+    if not os.path.exists(lib_path):
+        subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "port"], check=True)
+    cores = os.cpu_count() or 1
+    moff = np.concatenate([[0], np.cumsum(sizes_m)])
+    # sample size: roughly budget_s of work; calibrate on one QP per core
+    sample = min(len(probs), max(cores, 4 * cores))
+    idx = list(range(sample))
+    chunks = [idx[c::cores] for c in range(cores) if idx[c::cores]]
+    tasks = []
+    for ch in chunks:
+        pp = [probs[i] for i in ch]
+        lst = [[ls[s][moff[i]:moff[i + 1]] for i in ch] for s in range(steps)]
+        ust = [[us[s][moff[i]:moff[i + 1]] for i in ch] for s in range(steps)]
+        tasks.append((lib_path, pp, lst, ust))
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(len(tasks)) as pool:
+        res = pool.map(_cpu_worker, tasks)
+    wall = time.perf_counter() - t0
+    solved = sum(r[1] for r in res)
+    busy = max(r[0] for r in res)
+    objs = {}
+    for ch, r in zip(chunks, res):
+        for i, o in zip(ch, r[2]):
+            objs[i] = o
+    return {"value": solved / busy, "cores": len(tasks), "sample": f"{sample} MPC QPs x {steps} step(s)",
+            "wall_s": wall, "objs": objs}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def gpu_arm(args, probs, ls, us):
+    import torch
+    from osqp_gb300 import load
+    from osqp_gb300.api import Batch, OSQP
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    lib = load("f32")
+    settings = dict(SETTINGS, device=local)
+    b = Batch(lib)
+    rc = b.setup(probs, **settings)
+    assert rc == 0, f"batch setup failed: {rc}"
+    count = b.count
+    K, W = args.steps, args.warmup
+    nsteps = K + W
+    # bounds of every step resident in HBM (device path) and pinned on the host (e2e path)
+    dev_l = [torch.from_numpy(ls[s].astype(np.float32)).to(f"cuda:{local}") for s in range(nsteps)]
+    dev_u = [torch.from_numpy(us[s].astype(np.float32)).to(f"cuda:{local}") for s in range(nsteps)]
+    pin_l = [torch.from_numpy(ls[s].astype(np.float32)).pin_memory() for s in range(nsteps)]
+    pin_u = [torch.from_numpy(us[s].astype(np.float32)).pin_memory() for s in range(nsteps)]
+    x_out = torch.empty(b.nsum, dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-resident path ----
+    for s in range(W):
+        b.update_ptr(l_ptr=dev_l[s].data_ptr(), u_ptr=dev_u[s].data_ptr())
+        b.solve()
+    clocks = ClockSampler()
+    barrier(); torch.cuda.synchronize()
+    clocks.start()
+    step_ms, solve_ms, bytes_alg = [], [], 0.0
+    obj_first = None
+    admm_tot = pcg_tot = 0
+    nnz_pf = [pfull_nnz(p[0]) for p in probs]
+    launches = 0
+    for s in range(W, nsteps):
+        rc1 = b.update_ptr(l_ptr=dev_l[s].data_ptr(), u_ptr=dev_u[s].data_ptr())
+        rc2 = b.solve()
+        assert rc1 == 0 and rc2 == 0, (rc1, rc2)
+        launches += 4  # bounds check, update, solve, info kernels
+        step_ms.append(b.step_ms())
+        st = b.stats()
+        solve_ms.append(st["kernel_ms"])
+        sol = b.solution()
+        if obj_first is None:
+            obj_first = sol["obj"].copy()   # step W: the step the CPU sample solves
+        pcg = b.pcg_iters()
+        admm_tot += int(sol["iter"].sum()); pcg_tot += int(pcg.sum())
+        for k, (P, q, A, l, u) in enumerate(probs):
+            bytes_alg += solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, 4, int(sol["iter"][k]),
+                                     int(pcg[k]), SETTINGS["check_termination"])
+    torch.cuda.synchronize(); barrier()
+    clk = clocks.stop()
+    status_last = sol["status"].copy()
+    obj_last = sol["obj"].copy()
+    dev_total_ms = float(np.sum(step_ms))
+
+    # ---- end-to-end path through the C API from pinned host memory ----
+    barrier(); torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st_host = np.zeros(count, np.int32)
+    for s in range(W, nsteps):
+        b.update_ptr(l_ptr=pin_l[s].data_ptr(), u_ptr=pin_u[s].data_ptr())
+        b.solve()
+        b.solution_ptr(x_ptr=x_out.data_ptr())
+        st_host = b.statuses()
+    torch.cuda.synchronize(); barrier()
+    e2e_s = time.perf_counter() - t0
+
+    # ---- max over ranks ----
+    vals = np.array([dev_total_ms, e2e_s], dtype=np.float64)
+    if dist is not None:
+        t = torch.from_numpy(vals)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        vals = t.numpy()
+        dist.destroy_process_group()
+    dev_total_ms, e2e_s = float(vals[0]), float(vals[1])
+
+    # ---- plain one-QP-at-a-time GPU form on a sample (the reference's usage pattern) ----
+    plain = None
+    if rank == 0 and args.plain_sample > 0:
+        os.environ.setdefault("OSQP_GB300_MODE", "grid")
+        tt = 0.0
+        ns = min(args.plain_sample, count)
+        moff = np.concatenate([[0], np.cumsum([p[2].shape[0] for p in probs])])
+        for k in range(ns):
+            s1 = OSQP(lib)
+            s1.setup(*probs[k], **settings)
+            s1.update(l=ls[W][moff[k]:moff[k + 1]], u=us[W][moff[k]:moff[k + 1]])
+            t1 = time.perf_counter()
+            s1.solve()
+            tt += time.perf_counter() - t1
+            s1.cleanup()
+        plain = ns / tt
+
+    solves = count * K * world
+    out = dict(
+        value=solves / (dev_total_ms * 1e-3),
+        ms_per_step=dev_total_ms / K,
+        e2e_value=solves / e2e_s,
+        h2d=2 * 4 * int(b.msum), d2h=4 * int(b.nsum) + 40 * count,
+        solve_ms=float(np.mean(solve_ms)),
+        achieved_gbs=bytes_alg / K / (np.mean(solve_ms) * 1e-3) / 1e9,
+        bytes_per_launch=bytes_alg / K,
+        admm_per_qp=admm_tot / (count * K), pcg_per_qp=pcg_tot / (count * K),
+        status_counts={int(k): int(v) for k, v in zip(*np.unique(status_last, return_counts=True))},
+        obj_last=obj_first, launches=launches, clocks=clk, plain=plain, rank=rank, world=world,
+    )
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--count", type=int, default=4096)
+    ap.add_argument("--plain-sample", type=int, default=8)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    K, W = args.steps, args.warmup
+    config = {"workload": f"mpc_batch: {args.count} linear-MPC QPs (T~U{{10..50}}, nx~U{{8..40}}, nu~U{{4..16}}), "
+                          "new x0 per step, cold solve to eps 1e-3",
+              "qps_per_step": args.count, "eps": 1e-3, "settings": "rho_is_vec=1, check_termination=5, "
+              "adaptive_rho, scaling=10, check_dualgap=1", "l2": "inputs (~3 GB of CSR data) exceed the 129 MB L2",
+              "parallelism": f"replicas x{world}"}
+    metric = "QP solves/s (batched MPC, eps 1e-3)"
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        probs, ls, us = make_workload(args.count, 1)
+        sizes_m = [p[2].shape[0] for p in probs]
+        cpu = cpu_arm(probs, ls, us, sizes_m, budget_s=args.cpu_budget, steps=1)
+        line = dict(metric=metric, value=cpu["value"], unit="solves/s", n_gpus=args.gpus, steps=K, warmup=W,
+                    ms_per_step=args.count / cpu["value"] * 1e3, higher_is_better=True, scaling="weak",
+                    vs_baseline=None, dtype="f64", data="synthetic (seeded)", config=config, impl="reference",
+                    cpu_baseline={"value": cpu["value"], "unit": "solves/s", "cores": cpu["cores"], "kind": "port",
+                                  "sample": cpu["sample"]},
+                    e2e={"value": cpu["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+        print(json.dumps(line))
+        return
+
+    probs, ls, us = make_workload(args.count, K + W)
+    g = gpu_arm(args, probs, ls, us)
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    sizes_m = [p[2].shape[0] for p in probs]
+    cpu = cpu_arm(probs, [ls[W]], [us[W]], sizes_m, budget_s=args.cpu_budget, steps=1) if args.cpu_budget > 0 else None
+    # objective agreement with the FP64 oracle on the CPU sample (same QPs, same step)
+    obj_err = None
+    if cpu:
+        errs = []
+        for i, (stat, obj) in cpu["objs"].items():
+            if stat == 1 and i < len(g["obj_last"]):
+                errs.append(abs(float(g["obj_last"][i]) - obj) / max(1.0, abs(obj)))
+        obj_err = {"max_rel": float(np.max(errs)) if errs else None,
+                   "median_rel": float(np.median(errs)) if errs else None, "qps": len(errs)}
+    line = dict(
+        metric=metric, value=g["value"], unit="solves/s", n_gpus=world, steps=K, warmup=W,
+        ms_per_step=g["ms_per_step"], higher_is_better=True, scaling="weak", vs_baseline=None,
+        dtype="f32 (FP64-accurate double-float reductions)", data="synthetic (seeded)", config=config,
+        e2e={"value": g["e2e_value"], "unit": "solves/s", "h2d_bytes_per_step": g["h2d"],
+             "d2h_bytes_per_step": g["d2h"]},
+        roofline={"bound": "hbm", "achieved": g["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                  "frac": g["achieved_gbs"] / peak, "traffic": None,
+                  "kernel": "k_batch (solve)", "peak_source": peak_kind,
+                  "algorithmic_bytes_per_launch": g["bytes_per_launch"], "kernel_ms": g["solve_ms"]},
+        cpu_baseline=None if not cpu else {"value": cpu["value"], "unit": "solves/s", "cores": cpu["cores"],
+                                           "kind": "port", "sample": cpu["sample"]},
+        clocks=g["clocks"], gpu_launches=g["launches"],
+        plain_gpu_solves_per_s=g["plain"],
+        batched_over_plain=(g["value"] / g["plain"]) if g["plain"] else None,
+        admm_iters_per_qp=g["admm_per_qp"], pcg_iters_per_qp=g["pcg_per_qp"],
+        status_counts=g["status_counts"], objective_vs_fp64_oracle=obj_err,
+    )
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -62,6 +62,13 @@ OSQPInt osqp_gb300_batch_get_solution(OSQPBatch* batch, OSQPFloat* x, OSQPFloat*
 OSQPInt osqp_gb300_batch_stats(OSQPBatch* batch, double* kernel_ms, long long* admm_iter,
                                long long* pcg_iter);
 
+/* Device time (ms) from the start of the last osqp_gb300_batch_update_data_vec
+ * to the end of the following solve (equals the solve time without an update). */
+OSQPInt osqp_gb300_batch_step_ms(OSQPBatch* batch, double* step_ms);
+
+/* PCG iterations of every QP in the last batch solve (count entries, host memory). */
+OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* batch, long long* pcg_iter);
+
 OSQPInt osqp_gb300_batch_cleanup(OSQPBatch* batch);
 
 #ifdef __cplusplus

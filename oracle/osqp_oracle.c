@@ -646,15 +646,20 @@ static void update_status(OSQPInfo* info, OSQPInt s) {
   info->status[31] = 0;
 }
 
-/* ---- scaling (src/scaling.c:48-208) ---- */
+/* ---- scaling (src/scaling.c:48-208) ----
+ * Column inf-norms of P: the builtin algebra takes them over the stored upper
+ * triangle only (algebra/builtin/matrix.c:194-197 -> csc_col_norm_inf), the
+ * CUDA algebra over the full symmetric matrix (algebra/cuda/matrix.cu:130-135).
+ * The direct mode restates the builtin backend, the indirect mode the CUDA one. */
 static void scale_data(OSQPSolver* solver) {
   OSQPWorkspace* w = solver->work;
   OSQPInt n = w->n, m = w->m, i, k;
+  const int sym = solver->settings->linsys_solver == OSQP_INDIRECT_SOLVER;
   w->c = 1.0;
   for (k = 0; k < n; k++) { w->D[k] = 1.0; w->Dinv[k] = 1.0; }
   for (k = 0; k < m; k++) { w->E[k] = 1.0; w->Einv[k] = 1.0; }
   for (i = 0; i < solver->settings->scaling; i++) {
-    csc_col_norm_inf(w->P, w->D_temp, 1);
+    csc_col_norm_inf(w->P, w->D_temp, sym);
     csc_col_norm_inf(w->A, w->D_temp_A, 0);
     for (k = 0; k < n; k++) w->D_temp[k] = dmax(w->D_temp[k], w->D_temp_A[k]);
     csc_row_norm_inf(w->A, w->E_temp);
@@ -664,7 +669,7 @@ static void scale_data(OSQPSolver* solver) {
     csc_lmult(w->A, w->E_temp); csc_rmult(w->A, w->D_temp);
     for (k = 0; k < n; k++) { w->q[k] *= w->D_temp[k]; w->D[k] *= w->D_temp[k]; }
     for (k = 0; k < m; k++) w->E[k] *= w->E_temp[k];
-    csc_col_norm_inf(w->P, w->D_temp, 1);
+    csc_col_norm_inf(w->P, w->D_temp, sym);
     double ct = 0.0;
     for (k = 0; k < n; k++) ct += fabs(w->D_temp[k]);
     ct /= n;

@@ -318,6 +318,10 @@ class Batch:
         L.osqp_gb300_batch_stats.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                              C.POINTER(C.c_longlong)]
         L.osqp_gb300_batch_stats.restype = I
+        L.osqp_gb300_batch_step_ms.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.osqp_gb300_batch_step_ms.restype = I
+        L.osqp_gb300_batch_pcg_iters.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+        L.osqp_gb300_batch_pcg_iters.restype = I
         L.osqp_gb300_batch_cleanup.argtypes = [C.c_void_p]
         L.osqp_gb300_batch_cleanup.restype = I
 
@@ -381,6 +385,36 @@ class Batch:
     def split(self, v, which):
         sizes = self.packed["n"] if which == "n" else self.packed["m"]
         return np.split(v, np.cumsum(sizes)[:-1])
+
+    def statuses(self):
+        I = self.L.I
+        status = np.zeros(self.count, np.int32)
+        rc = self.L.lib.osqp_gb300_batch_get_solution(self._h, None, None, _ptr(status, I), None, None, None, None)
+        assert rc == 0, rc
+        return status
+
+    def step_ms(self) -> float:
+        v = C.c_double()
+        self.L.lib.osqp_gb300_batch_step_ms(self._h, C.byref(v))
+        return v.value
+
+    def update_ptr(self, l_ptr=0, u_ptr=0, q_ptr=0) -> int:
+        """update() from raw (host or device) addresses, e.g. torch tensors' data_ptr()."""
+        PF = C.POINTER(self.L.F)
+        cast = lambda a: C.cast(C.c_void_p(a), PF) if a else None
+        return int(self.L.lib.osqp_gb300_batch_update_data_vec(self._h, cast(q_ptr), cast(l_ptr), cast(u_ptr)))
+
+    def solution_ptr(self, x_ptr=0, y_ptr=0) -> int:
+        """Copy packed x / y to raw (host or device) addresses."""
+        PF = C.POINTER(self.L.F)
+        cast = lambda a: C.cast(C.c_void_p(a), PF) if a else None
+        return int(self.L.lib.osqp_gb300_batch_get_solution(self._h, cast(x_ptr), cast(y_ptr), None, None,
+                                                            None, None, None))
+
+    def pcg_iters(self):
+        out = np.zeros(self.count, np.int64)
+        self.L.lib.osqp_gb300_batch_pcg_iters(self._h, out.ctypes.data_as(C.POINTER(C.c_longlong)))
+        return out
 
     def stats(self):
         ms, a, p = C.c_double(), C.c_longlong(), C.c_longlong()

@@ -3,8 +3,11 @@
     python -m osqp_gb300.build            # both precisions, in parallel
 
 Outputs (git-ignored, next to this file):
-    osqp_gb300/lib/libosqp_gb300.so        OSQPFloat = float  (the reference CUDA default)
-    osqp_gb300/lib/libosqp_gb300_f64.so    OSQPFloat = double
+    osqp_gb300/lib/libosqp_gb300.so                OSQP public API + batch engine, OSQPFloat = float
+    osqp_gb300/lib/libosqp_gb300_f64.so            the same with OSQPFloat = double
+    osqp_gb300/lib/libosqp_gb300_algebra.so        algebra / linear-system ABI (drop-in for the
+                                                   reference's algebra/cuda), OSQPFloat = float
+    osqp_gb300/lib/libosqp_gb300_algebra_f64.so    the same with OSQPFloat = double
 Each translation unit is compiled once per precision; all compilations run
 concurrently and are skipped when the object is newer than its sources.
 """
@@ -27,13 +30,18 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--extended-lambda", "-Xcompiler", "-fPIC",
            "-I" + INCLUDE, "-I" + CSRC]
 
-# translation units of each library
-SOURCES = ["engine.cu", "polish.cu", "batch.cu", "algebra.cu"]
-
 VARIANTS = {
-    "f32": {"defines": ["-DOSQP_USE_FLOAT"], "lib": "libosqp_gb300.so"},
-    "f64": {"defines": [], "lib": "libosqp_gb300_f64.so"},
+    "f32": {"defines": ["-DOSQP_USE_FLOAT"]},
+    "f64": {"defines": []},
 }
+# library -> (precision variant, translation units)
+TARGETS = {
+    "libosqp_gb300.so": ("f32", ["engine.cu", "polish.cu", "batch.cu"]),
+    "libosqp_gb300_f64.so": ("f64", ["engine.cu", "polish.cu", "batch.cu"]),
+    "libosqp_gb300_algebra.so": ("f32", ["algebra.cu"]),
+    "libosqp_gb300_algebra_f64.so": ("f64", ["algebra.cu"]),
+}
+SOURCES = sorted({s for _, srcs in TARGETS.values() for s in srcs})
 
 
 def nvcc():
@@ -66,28 +74,28 @@ def _compile(src, variant):
     return obj, r.stderr
 
 
-def build(verbose: bool = False, sources=None) -> dict:
-    sources = [s for s in (sources or SOURCES) if os.path.exists(os.path.join(CSRC, s))]
+def build(verbose: bool = False) -> dict:
     os.makedirs(LIB, exist_ok=True)
-    jobs = [(s, v) for v in VARIANTS for s in sources]
-    objs = {v: [] for v in VARIANTS}
+    jobs = sorted({(src, v) for v, srcs in TARGETS.values() for src in srcs})
+    objs = {}
     with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
         futs = {ex.submit(_compile, s, v): (s, v) for s, v in jobs}
         for f in cf.as_completed(futs):
-            s, v = futs[f]
+            key = futs[f]
             obj, log = f.result()
-            objs[v].append(obj)
+            objs[key] = obj
             if verbose and log:
                 print(log)
     out = {}
-    for v, spec in VARIANTS.items():
-        lib = os.path.join(LIB, spec["lib"])
-        if _stale(lib, objs[v]):
-            cmd = [nvcc()] + ARCH + ["-shared", "-Xlinker", "-Bsymbolic", "-o", lib] + sorted(objs[v]) + ["-lcudart"]
+    for name, (v, srcs) in TARGETS.items():
+        lib = os.path.join(LIB, name)
+        deps = [objs[(s, v)] for s in srcs]
+        if _stale(lib, deps):
+            cmd = [nvcc()] + ARCH + ["-shared", "-Xlinker", "-Bsymbolic", "-o", lib] + deps + ["-lcudart"]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError(f"link failed for {lib}:\n{r.stderr[-4000:]}")
-        out[v] = lib
+        out[name] = lib
     return out
 
 

@@ -205,12 +205,13 @@ __global__ void k_batch_check_bounds(const TT* l, const TT* u, long long msum, i
     if (l[j] > u[j]) atomicExch(bad, 1);
 }
 
-struct BatchInfo { int status, iter; double obj, prim, dual; };
+struct BatchInfo { int status, iter; long long pcg; double obj, prim, dual; };
 
 __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out, long long* totals) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
     out[k].status = st[k].status;
     out[k].iter = st[k].iter;
+    out[k].pcg = st[k].pcg_iters_total;
     out[k].obj = st[k].obj_val;
     out[k].prim = st[k].prim_res;
     out[k].dual = st[k].dual_res;
@@ -230,7 +231,8 @@ struct OSQPBatch_ {
   int count, device;
   long long nsum, msum, nnzT, nnzA, nnzPf;
   cudaStream_t stream;
-  cudaEvent_t ev0, ev1;
+  cudaEvent_t ev0, ev1, evu;
+  int upd_pending;
   char* arena;
   BatchArrays<T> B;
   BatchInst* d_inst;
@@ -243,7 +245,7 @@ struct OSQPBatch_ {
   DevSettings ds;
   OSQPSettings settings;
   int grid;
-  float last_ms;
+  float last_ms, last_step_ms;
   long long last_admm, last_pcg;
   std::vector<BatchInst> inst;
 };
@@ -282,6 +284,7 @@ extern "C" OSQPInt osqp_gb300_batch_cleanup(OSQPBatch* b) {
   if (b->arena) cudaFree(b->arena);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->evu) cudaEventDestroy(b->evu);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return 0;
@@ -375,7 +378,8 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
 
   // ---- arena ----
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+      cudaEventCreate(&b->evu) != cudaSuccess) {
     osqp_gb300_batch_cleanup(b); return OSQP_ALGEBRA_LOAD_ERROR;
   }
   struct Plan { size_t off = 0; size_t take(size_t bytes) { off = (off + 255) & ~size_t(255); size_t o = off; off += bytes > 0 ? bytes : 1; return o; } } pl;
@@ -494,6 +498,8 @@ extern "C" OSQPInt osqp_gb300_batch_update_data_vec(OSQPBatch* b, const OSQPFloa
   cudaSetDevice(b->device);
   cudaStream_t s = b->stream;
   BatchArrays<T>& B = b->B;
+  cudaEventRecord(b->evu, s);
+  b->upd_pending = 1;
   if (l || u) {
     BT_TRY(cudaMemcpyAsync(b->stage_l, l ? (const void*)l : (const void*)B.vm[2], sizeof(T) * b->msum,
                            l ? cudaMemcpyDefault : cudaMemcpyDeviceToDevice, s));
@@ -526,6 +532,9 @@ extern "C" OSQPInt osqp_gb300_batch_solve(OSQPBatch* b) {
   BT_TRY(cudaMemcpyAsync(tot, b->d_totals, sizeof(tot), cudaMemcpyDeviceToHost, b->stream));
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return OSQP_ALGEBRA_LOAD_ERROR;
   cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+  if (b->upd_pending) cudaEventElapsedTime(&b->last_step_ms, b->evu, b->ev1);
+  else b->last_step_ms = b->last_ms;
+  b->upd_pending = 0;
   b->last_admm = tot[0]; b->last_pcg = tot[1];
   return 0;
 }
@@ -550,6 +559,20 @@ extern "C" OSQPInt osqp_gb300_batch_get_solution(OSQPBatch* b, OSQPFloat* x, OSQ
     }
   }
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : OSQP_ALGEBRA_LOAD_ERROR;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_step_ms(OSQPBatch* b, double* step_ms) {
+  if (!b || !step_ms) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  *step_ms = b->last_step_ms;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* b, long long* pcg) {
+  if (!b || !pcg) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  std::vector<BatchInfo> info(b->count);
+  BT_TRY(cudaMemcpy(info.data(), b->d_info, sizeof(BatchInfo) * b->count, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < b->count; k++) pcg[k] = info[k].pcg;
+  return 0;
 }
 
 extern "C" OSQPInt osqp_gb300_batch_stats(OSQPBatch* b, double* kernel_ms, long long* admm_iter, long long* pcg_iter) {

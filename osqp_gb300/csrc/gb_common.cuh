@@ -308,6 +308,56 @@ struct CSR {
   int lanes;  // lanes per row: 1,2,4,8,16,32
 };
 
+
+// Dot product of one CSR row segment handled by a sub-warp lane: entries
+// b+sl, b+sl+L, ... < e.  Four entries are fetched per round before any is
+// used, so each lane keeps four index/value loads and four gathers in flight.
+template <int L, typename T, typename XF>
+__device__ __forceinline__ T lane_row_dot(const int* __restrict__ col, const T* __restrict__ val,
+                                          int b, int e, int sl, XF xf) {
+  T acc = T(0);
+  for (int k0 = b + sl; k0 < e; k0 += 4 * L) {
+    int c[4];
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int k = k0 + u * L;
+      c[u] = k < e ? col[k] : -1;
+      v[u] = k < e ? val[k] : T(0);
+    }
+    T x[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) x[u] = c[u] >= 0 ? xf(c[u]) : T(0);
+#pragma unroll
+    for (int u = 0; u < 4; u++) acc += v[u] * x[u];
+  }
+  return acc;
+}
+
+// Two products of the same row (shared index and value loads).
+template <int L, typename T, typename XF1, typename XF2>
+__device__ __forceinline__ void lane_row_dot2(const int* __restrict__ col, const T* __restrict__ val,
+                                              int b, int e, int sl, XF1 xf1, XF2 xf2, T& a1, T& a2) {
+  for (int k0 = b + sl; k0 < e; k0 += 4 * L) {
+    int c[4];
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int k = k0 + u * L;
+      c[u] = k < e ? col[k] : -1;
+      v[u] = k < e ? val[k] : T(0);
+    }
+    T x1[4], x2[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      x1[u] = c[u] >= 0 ? xf1(c[u]) : T(0);
+      x2[u] = c[u] >= 0 ? xf2(c[u]) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) { a1 += v[u] * x1[u]; a2 += v[u] * x2[u]; }
+  }
+}
+
 // Visit every row of M; each sub-warp of L lanes computes sum_k val[k]*xf(col[k])
 // for its row and calls fn(row, dot) on the sub-warp's lane 0.  Warp-uniform
 // loop trip counts keep every shuffle convergent.
@@ -320,10 +370,7 @@ __device__ __forceinline__ void rows_apply_L(G& g, const CSR<T>& M, XF xf, FN fn
   for (int base = w * RPW; base < M.rows; base += nw * RPW) {
     const int r = base + sub;
     T acc = T(0);
-    if (r < M.rows) {
-      const int b = M.rowptr[r], e = M.rowptr[r + 1];
-      for (int k = b + sl; k < e; k += L) acc += M.val[k] * xf(M.col[k]);
-    }
+    if (r < M.rows) acc = lane_row_dot<L>(M.col, M.val, M.rowptr[r], M.rowptr[r + 1], sl, xf);
     acc = subwarp_sum<L>(acc);
     if (r < M.rows && sl == 0) fn(r, acc);
   }
@@ -351,15 +398,7 @@ __device__ __forceinline__ void rows_apply2_L(G& g, const CSR<T>& M, XF1 xf1, XF
   for (int base = w * RPW; base < M.rows; base += nw * RPW) {
     const int r = base + sub;
     T a1 = T(0), a2 = T(0);
-    if (r < M.rows) {
-      const int b = M.rowptr[r], e = M.rowptr[r + 1];
-      for (int k = b + sl; k < e; k += L) {
-        const int c = M.col[k];
-        const T v = M.val[k];
-        a1 += v * xf1(c);
-        a2 += v * xf2(c);
-      }
-    }
+    if (r < M.rows) lane_row_dot2<L>(M.col, M.val, M.rowptr[r], M.rowptr[r + 1], sl, xf1, xf2, a1, a2);
     a1 = subwarp_sum<L>(a1);
     a2 = subwarp_sum<L>(a2);
     if (r < M.rows && sl == 0) fn(r, a1, a2);
@@ -377,12 +416,13 @@ __device__ __forceinline__ void rows_apply2(G& g, const CSR<T>& M, XF1 a, XF2 b,
   }
 }
 
-// Lanes per row from the mean row length (power of two, 1..32).
+// Lanes per row from the mean row length: about four entries per lane
+// (power of two, 1..32), so short rows pack several rows into a warp.
 inline int pick_lanes(long long nnz, int rows) {
   if (rows <= 0) return 1;
-  double mean = (double)nnz / rows;
+  const double mean = (double)nnz / rows;
   int L = 1;
-  while (L < 32 && L < mean * 0.75) L <<= 1;
+  while (L < 32 && L * 4 < mean) L <<= 1;
   return L;
 }
 

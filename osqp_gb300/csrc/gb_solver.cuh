@@ -122,10 +122,8 @@ __device__ __forceinline__ void kkt_rows_L(G& g, const CSR<T>& P, const CSR<T>& 
     const int i = base + sub;
     T a1 = T(0), a2 = T(0);
     if (i < n) {
-      int b = P.rowptr[i], e = P.rowptr[i + 1];
-      for (int k = b + sl; k < e; k += L) a1 += P.val[k] * xp(P.col[k]);
-      b = At.rowptr[i]; e = At.rowptr[i + 1];
-      for (int k = b + sl; k < e; k += L) a2 += At.val[k] * xa(At.col[k]);
+      a1 = lane_row_dot<L>(P.col, P.val, P.rowptr[i], P.rowptr[i + 1], sl, xp);
+      a2 = lane_row_dot<L>(At.col, At.val, At.rowptr[i], At.rowptr[i + 1], sl, xa);
     }
     a1 = subwarp_sum<L>(a1);
     a2 = subwarp_sum<L>(a2);
@@ -397,80 +395,9 @@ struct Solver {
     __syncthreads();
     const double eps = sc->pcg_eps;
 
-    // Phase I: r = K xp - rhs, yv = M^-1 r, p = -yv, rTy, ||r||
-    T* pA = sc->p_parity ? pr.p1 : pr.p0;
-    Acc<T> sm1[1];
-    T mx1[1] = {T(0)};
-    kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return xp[c]; }, [&](int c) { return m ? pr.t[c] : T(0); },
-      [&](int i, T pv, T av) {
-        const T kx = sig * xp[i] + pv + av;
-        const T r = kx - pr.rhs[i];
-        const T yv = pr.Minv[i] * r;
-        pr.r[i] = r; pr.yv[i] = yv; pA[i] = -yv;
-        sm1[0].add_prod(yv, r);
-        mx1[0] = tmax(mx1[0], (T)fabs(r));
-      });
-    double rs1[1], rm1[1];
-    g.reduce(sm1, mx1, rs1, rm1);
-    if (!g.ok()) return false;
-    double rTy = rs1[0], rnorm = rm1[0];
-
-    // PCG loop (cuda_pcg.cu:155-200).  Four phases per iteration; each ends
-    // at a group barrier (the two reductions carry theirs).
-    T* p = pA;
-    int it = 0;
-    while (rnorm > eps && it < s.cg_max_iter) {
-      // Phase A: t = rho .* (A p)
-      if (m > 0) {
-        rows_apply(g, pr.A, [&](int c) { return p[c]; },
-                   [&](int j, T v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
-        if (!g.sync()) return false;
-      }
-      // Phase B: Kp = sigma p + P p + A' t ; pKp
-      Acc<T> sm2[1];
-      T mx2[1] = {T(0)};
-      kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return p[c]; }, [&](int c) { return m ? pr.t[c] : T(0); },
-        [&](int i, T pv, T av) {
-          const T pi = p[i];
-          const T kp = sig * pi + pv + av;
-          pr.Kp[i] = kp;
-          sm2[0].add_prod(pi, kp);
-        });
-      double rs2[1], rm2[1];
-      g.reduce(sm2, mx2, rs2, rm2);
-      if (!g.ok()) return false;
-      const double alpha = rTy / rs2[0];
-      const T at = (T)alpha;
-      // Phase C: x += alpha p ; r += alpha Kp ; yv = M^-1 r ; rTy ; ||r||
-      Acc<T> sm3[1];
-      T mx3[1] = {T(0)};
-      for_each(g, n, [&](int i) {
-        xp[i] += at * p[i];
-        const T r = pr.r[i] + at * pr.Kp[i];
-        pr.r[i] = r;
-        const T yv = pr.Minv[i] * r;
-        pr.yv[i] = yv;
-        sm3[0].add_prod(yv, r);
-        mx3[0] = tmax(mx3[0], (T)fabs(r));
-      });
-      double rs3[1], rm3[1];
-      g.reduce(sm3, mx3, rs3, rm3);
-      if (!g.ok()) return false;
-      const double rTy_new = rs3[0];
-      const double beta = rTy_new / rTy;
-      rTy = rTy_new;
-      rnorm = rm3[0];
-      it++;
-      // Phase D: p = beta p - yv (skipped when the loop is about to end)
-      if (rnorm > eps && it < s.cg_max_iter) {
-        const T bt = (T)beta;
-        for_each(g, n, [&](int i) { p[i] = bt * p[i] - pr.yv[i]; });
-        if (!g.sync()) return false;
-      }
-    }
+    const int pcg_it = pcg_core(g, eps, sig, rho_s);
+    if (pcg_it < 0) return false;
     if (threadIdx.x == 0) {
-      sc->pcg_iters_total += it;
-      if (it == 0) sc->zero_pcg_iters++; else sc->zero_pcg_iters = 0;
       sc->elapsed = elapsed;
       sc->cancel = cancel;
     }
@@ -498,6 +425,154 @@ struct Solver {
       });
     }
     __syncthreads();
+    return g.sync();
+  }
+
+
+  // ---------------------------------------------------------------------
+  // PCG on the reduced KKT system K = P + sigma I + A' R A from the current
+  // iterate xp and right-hand side rhs (cuda_pcg.cu:113-208): start-up
+  // product r = K xp - rhs, then four phases per iteration.  t holds
+  // R A p between phases.  Returns the iteration count, -1 on a barrier error.
+  // ---------------------------------------------------------------------
+  template <typename G>
+  __device__ int pcg_core(G& g, double eps, T sig, T rho_s) {
+    const int n = pr.n, m = pr.m;
+    const bool vec = s.rho_is_vec && pr.rho_vec;
+    T* __restrict__ xp = pr.xp;
+    // Phase I: r = K xp - rhs, yv = M^-1 r, p = -yv, rTy, ||r||
+    T* pA = sc->p_parity ? pr.p1 : pr.p0;
+    Acc<T> sm1[1];
+    T mx1[1] = {T(0)};
+    kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return xp[c]; }, [&](int c) { return m ? pr.t[c] : T(0); },
+      [&](int i, T pv, T av) {
+        const T kx = sig * xp[i] + pv + av;
+        const T r = kx - pr.rhs[i];
+        const T yv = pr.Minv[i] * r;
+        pr.r[i] = r; pr.yv[i] = yv; pA[i] = -yv;
+        sm1[0].add_prod(yv, r);
+        mx1[0] = tmax(mx1[0], (T)fabs(r));
+      });
+    double rs1[1], rm1[1];
+    g.reduce(sm1, mx1, rs1, rm1);
+    if (!g.ok()) return -1;
+    double rTy = rs1[0], rnorm = rm1[0];
+
+    // PCG loop (cuda_pcg.cu:155-200).  Four phases per iteration; each ends
+    // at a group barrier (the two reductions carry theirs).
+    T* p = pA;
+    int it = 0;
+    while (rnorm > eps && it < s.cg_max_iter) {
+      // Phase A: t = rho .* (A p)
+      if (m > 0) {
+        rows_apply(g, pr.A, [&](int c) { return p[c]; },
+                   [&](int j, T v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
+        if (!g.sync()) return -1;
+      }
+      // Phase B: Kp = sigma p + P p + A' t ; pKp
+      Acc<T> sm2[1];
+      T mx2[1] = {T(0)};
+      kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return p[c]; }, [&](int c) { return m ? pr.t[c] : T(0); },
+        [&](int i, T pv, T av) {
+          const T pi = p[i];
+          const T kp = sig * pi + pv + av;
+          pr.Kp[i] = kp;
+          sm2[0].add_prod(pi, kp);
+        });
+      double rs2[1], rm2[1];
+      g.reduce(sm2, mx2, rs2, rm2);
+      if (!g.ok()) return -1;
+      const double alpha = rTy / rs2[0];
+      const T at = (T)alpha;
+      // Phase C: x += alpha p ; r += alpha Kp ; yv = M^-1 r ; rTy ; ||r||
+      Acc<T> sm3[1];
+      T mx3[1] = {T(0)};
+      for_each(g, n, [&](int i) {
+        xp[i] += at * p[i];
+        const T r = pr.r[i] + at * pr.Kp[i];
+        pr.r[i] = r;
+        const T yv = pr.Minv[i] * r;
+        pr.yv[i] = yv;
+        sm3[0].add_prod(yv, r);
+        mx3[0] = tmax(mx3[0], (T)fabs(r));
+      });
+      double rs3[1], rm3[1];
+      g.reduce(sm3, mx3, rs3, rm3);
+      if (!g.ok()) return -1;
+      const double rTy_new = rs3[0];
+      const double beta = rTy_new / rTy;
+      rTy = rTy_new;
+      rnorm = rm3[0];
+      it++;
+      // Phase D: p = beta p - yv (skipped when the loop is about to end)
+      if (rnorm > eps && it < s.cg_max_iter) {
+        const T bt = (T)beta;
+        for_each(g, n, [&](int i) { p[i] = bt * p[i] - pr.yv[i]; });
+        if (!g.sync()) return -1;
+      }
+    }
+    if (threadIdx.x == 0) {
+      sc->pcg_iters_total += it;
+      if (it == 0) sc->zero_pcg_iters++; else sc->zero_pcg_iters = 0;
+    }
+    __syncthreads();
+    return it;
+
+  }
+
+  // Reduced-KKT solve behind the linear-system interface (LinSysSolver.solve,
+  // cuda_pcg_interface.cu:229-273): b = [b1; b2] in, [x~; A x~] out
+  // (polishing: [x; (A x - b2) / delta]).  The CG tolerance follows
+  // cuda_pcg_interface.cu:32-64 with the caller's scaled residuals.
+  template <typename G>
+  __device__ bool linsys_solve(G& g, T* b, int admm_iter, bool polishing, double spr, double sdr) {
+    const int n = pr.n, m = pr.m;
+    const bool vec = s.rho_is_vec && pr.rho_vec;
+    const T sig = (T)s.sigma;
+    const T rho_s = (T)sc->rho;
+    T* __restrict__ xp = pr.xp;
+    const T* b1 = b;
+    T* b2 = b + n;
+    Acc<T> sm0[1];
+    T mx0[1] = {T(0)};
+    rows_apply(g, pr.At, [&](int j) { return (vec ? pr.rho_vec[j] : rho_s) * b2[j]; },
+               [&](int i, T v) {
+                 const T rr = b1[i] + v;
+                 pr.rhs[i] = rr;
+                 mx0[0] = tmax(mx0[0], (T)fabs(rr));
+               });
+    if (m > 0)
+      rows_apply(g, pr.A, [&](int c) { return xp[c]; },
+                 [&](int j, T v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
+    double rs0[1], rm0[1];
+    g.reduce(sm0, mx0, rs0, rm0);
+    if (!g.ok()) return false;
+    const double rhs_norm = rm0[0];
+    if (threadIdx.x == 0) {
+      double e;
+      if (polishing) e = fmax(rhs_norm * 1e-5, kCgTolMin);
+      else if (admm_iter == 1) {
+        sc->reduction_factor = s.cg_tol_fraction;
+        sc->eps_prev = rhs_norm < kCgTolMin ? 1.0 : rhs_norm * sc->reduction_factor;
+        e = sc->eps_prev;
+      } else {
+        if (sc->zero_pcg_iters >= s.cg_tol_reduction) { sc->reduction_factor /= 2; sc->zero_pcg_iters = 0; }
+        e = sc->reduction_factor * sqrt(spr * sdr);
+        e = fmax(fmin(e, sc->eps_prev), kCgTolMin);
+        sc->eps_prev = e;
+      }
+      sc->pcg_eps = e;
+    }
+    __syncthreads();
+    const double eps = sc->pcg_eps;
+    if (pcg_core(g, eps, sig, rho_s) < 0) return false;
+    // outputs: b1 <- x ; b2 <- A x  (or (A x - b2) / delta when polishing)
+    for_each(g, n, [&](int i) { b[i] = xp[i]; });
+    if (m > 0) {
+      const T rp = (T)sc->rho;
+      rows_apply(g, pr.A, [&](int c) { return xp[c]; },
+                 [&](int j, T v) { b2[j] = polishing ? (v - b2[j]) * rp : v; });
+    }
     return g.sync();
   }
 
@@ -582,16 +657,10 @@ struct Solver {
           const int i = base + sub;
           T px = T(0), pdx = T(0), aty = T(0), atdy = T(0);
           if (i < n) {
-            int b = pr.P.rowptr[i], e = pr.P.rowptr[i + 1];
-            for (int k = b + sl; k < e; k += LL) {
-              const T v = pr.P.val[k]; const int c = pr.P.col[k];
-              px += v * x[c]; pdx += v * pr.dx[c];
-            }
-            b = pr.At.rowptr[i]; e = pr.At.rowptr[i + 1];
-            for (int k = b + sl; k < e; k += LL) {
-              const T v = pr.At.val[k]; const int c = pr.At.col[k];
-              aty += v * y[c]; atdy += v * pr.dy[c];
-            }
+            lane_row_dot2<LL>(pr.P.col, pr.P.val, pr.P.rowptr[i], pr.P.rowptr[i + 1], sl,
+                              [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; }, px, pdx);
+            lane_row_dot2<LL>(pr.At.col, pr.At.val, pr.At.rowptr[i], pr.At.rowptr[i + 1], sl,
+                              [&](int c) { return y[c]; }, [&](int c) { return pr.dy[c]; }, aty, atdy);
           }
           px = subwarp_sum<LL>(px); pdx = subwarp_sum<LL>(pdx);
           aty = subwarp_sum<LL>(aty); atdy = subwarp_sum<LL>(atdy);
