@@ -16,7 +16,8 @@ extern "C" {
 
 /* Statistics of the last osqp_solve: ADMM iterations, total PCG iterations,
  * device time of the solve kernel (ms) and the execution form used
- * (0 = one CTA, 1 = cooperative grid).  Returns 0 on success. */
+ * (0 = one CTA, 1 = cooperative grid, k > 1 = one cluster of k CTAs).
+ * Returns 0 on success. */
 OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter, long long* pcg_iter,
                                double* kernel_ms, OSQPInt* grid_form);
 

@@ -26,6 +26,7 @@
 #include "osqp_gb300_ext.h"
 #include "gb_solver.cuh"
 #include "gb_structure.cuh"
+#include "gb_launch.cuh"
 
 using T = OSQPFloat;
 using namespace gb;
@@ -88,7 +89,39 @@ struct BatchArrays {
 
 enum BatchMode : int { kModeSetup = 0, kModeSolve = 1, kModeUpdateVec = 2 };
 
-// Persistent kernel: each CTA pulls QPs from the queue and runs `mode` on them.
+// Work on one QP by a group (a CTA, or the CTAs of a cluster).
+template <typename TT, typename G>
+__device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s, int k, int mode,
+                           GroupShared& gsh, SolverScalars& ssc) {
+  DevProblem<TT> pr = B.problem(k);
+  if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pr.st; }
+  __syncthreads();
+  Solver<TT> S{pr, s, &ssc, B.inst[k].kktL};
+  if (mode == kModeSetup) {
+    S.setup(g);
+  } else if (mode == kModeSolve) {
+    S.solve(g);
+  } else {
+    // new q / l / u from *_in with the QP's existing scaling (osqp_api.c:1184-1257)
+    const TT c = (TT)ssc.c;
+    const bool sc_on = s.scaling != 0;
+    for_each(g, pr.n, [&](int i) { pr.q[i] = sc_on ? (pr.q_in[i] * pr.D[i]) * c : pr.q_in[i]; });
+    for_each(g, pr.m, [&](int j) {
+      pr.l[j] = sc_on ? pr.l_in[j] * pr.E[j] : pr.l_in[j];
+      pr.u[j] = sc_on ? pr.u_in[j] * pr.E[j] : pr.u_in[j];
+    });
+    g.sync();
+    if (s.rho_is_vec) {
+      S.set_rho_vec(g);
+      g.sync();
+      S.update_precond(g);
+    }
+    if (threadIdx.x == 0) { ssc.status = ST_UNSOLVED; ssc.rho_updates = 0; }
+  }
+  g.sync();
+}
+
+// Persistent kernel, one CTA per QP: CTAs pull QPs from the queue.
 template <typename TT>
 __global__ void __launch_bounds__(kBatchThreads, 2)
 k_batch(BatchArrays<TT> B, DevSettings s, int count, int* queue, const int* order, int mode) {
@@ -100,36 +133,33 @@ k_batch(BatchArrays<TT> B, DevSettings s, int count, int* queue, const int* orde
     if (threadIdx.x == 0) s_idx = atomicAdd(queue, 1);
     __syncthreads();
     const int idx = s_idx;
+    __syncthreads();
     if (idx >= count) break;
-    const int k = order[idx];
-    DevProblem<TT> pr = B.problem(k);
-    if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pr.st; }
+    batch_item(g, B, s, order[idx], mode, gsh, ssc);
+    if (threadIdx.x == 0) *B.problem(order[idx]).st = ssc;
     __syncthreads();
-    Solver<TT> S{pr, s, &ssc, B.inst[k].kktL};
-    if (mode == kModeSetup) {
-      S.setup(g);
-    } else if (mode == kModeSolve) {
-      S.solve(g);
-    } else {
-      // new q / l / u from *_in with the QP's existing scaling (osqp_api.c:1184-1257)
-      const TT c = (TT)ssc.c;
-      const bool sc_on = s.scaling != 0;
-      for_each(g, pr.n, [&](int i) { pr.q[i] = sc_on ? (pr.q_in[i] * pr.D[i]) * c : pr.q_in[i]; });
-      for_each(g, pr.m, [&](int j) {
-        pr.l[j] = sc_on ? pr.l_in[j] * pr.E[j] : pr.l_in[j];
-        pr.u[j] = sc_on ? pr.u_in[j] * pr.E[j] : pr.u_in[j];
-      });
-      __syncthreads();
-      if (s.rho_is_vec) {
-        S.set_rho_vec(g);
-        __syncthreads();
-        S.update_precond(g);
-      }
-      if (threadIdx.x == 0) { ssc.status = ST_UNSOLVED; ssc.rho_updates = 0; }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) *pr.st = ssc;
-    __syncthreads();
+  }
+}
+
+// Persistent kernel, one thread-block cluster per QP: the cluster's rank-0 CTA
+// pulls a QP and broadcasts it through distributed shared memory.
+template <typename TT>
+__global__ void __launch_bounds__(kBatchThreads, 1)
+k_batch_cluster(BatchArrays<TT> B, DevSettings s, int count, int* queue, const int* order, int mode) {
+  namespace cgr = cooperative_groups;
+  __shared__ GroupShared gsh;
+  __shared__ SolverScalars ssc;
+  cgr::cluster_group cl = cgr::this_cluster();
+  ClusterGroup g{&gsh, cl.block_rank(), cl.num_blocks()};
+  for (;;) {
+    if (g.rank == 0 && threadIdx.x == 0) gsh.cidx = atomicAdd(queue, 1);
+    cl.sync();
+    const int idx = *cl.map_shared_rank(&gsh.cidx, 0);
+    cl.sync();   // rank 0 keeps its shared memory until every CTA has read idx
+    if (idx >= count) break;
+    batch_item(g, B, s, order[idx], mode, gsh, ssc);
+    if (g.rank == 0 && threadIdx.x == 0) *B.problem(order[idx]).st = ssc;
+    cl.sync();
   }
 }
 
@@ -245,6 +275,7 @@ struct OSQPBatch_ {
   DevSettings ds;
   OSQPSettings settings;
   int grid;
+  int cluster;   // CTAs per QP (1 = one CTA per QP)
   float last_ms, last_step_ms;
   long long last_admm, last_pcg;
   std::vector<BatchInst> inst;
@@ -274,8 +305,13 @@ static DevSettings batch_dev_settings(const OSQPSettings* st) {
 
 static int run_batch_kernel(OSQPBatch* b, int mode) {
   BT_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream));
-  k_batch<T><<<b->grid, kBatchThreads, 0, b->stream>>>(b->B, b->ds, b->count, b->d_queue, b->d_order, mode);
-  BT_TRY(cudaGetLastError());
+  if (b->cluster > 1) {
+    BT_TRY(launch_clusters(k_batch_cluster<T>, b->grid, b->cluster, kBatchThreads, b->stream,
+                           b->B, b->ds, b->count, b->d_queue, (const int*)b->d_order, mode));
+  } else {
+    k_batch<T><<<b->grid, kBatchThreads, 0, b->stream>>>(b->B, b->ds, b->count, b->d_queue, b->d_order, mode);
+    BT_TRY(cudaGetLastError());
+  }
   return 0;
 }
 
@@ -479,11 +515,20 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   }
   cudaFreeAsync(dPp, s); cudaFreeAsync(dAp, s); cudaFreeAsync(dppoff, s); cudaFreeAsync(dPi, s);
 
-  // ---- persistent grid: SMs x resident CTAs ----
+  // ---- persistent grid: SMs x resident CTAs, or resident clusters ----
   int per_sm = 0, sms = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<T>, kBatchThreads, 0);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-  b->grid = std::max(1, std::min(count, sms * std::max(per_sm, 1)));
+  const char* cenv = getenv("OSQP_GB300_BATCH_CLUSTER");
+  b->cluster = cenv ? std::max(1, std::min(16, atoi(cenv))) : 1;
+  if (b->cluster > 1) {
+    int nclusters = max_active_clusters(k_batch_cluster<T>, b->cluster, kBatchThreads);
+    if (nclusters < 1) b->cluster = 1;
+    else b->grid = std::max(1, std::min(count, nclusters));   // grid counted in clusters
+  }
+  if (b->cluster <= 1) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<T>, kBatchThreads, 0);
+    b->grid = std::max(1, std::min(count, sms * std::max(per_sm, 1)));
+  }
 
   int rc = run_batch_kernel(b, kModeSetup);
   if (rc) { osqp_gb300_batch_cleanup(b); return rc; }

@@ -23,6 +23,7 @@
 #include "osqp_gb300_ext.h"
 #include "gb_solver.cuh"
 #include "gb_structure.cuh"
+#include "gb_launch.cuh"
 
 using T = OSQPFloat;
 using namespace gb;
@@ -103,6 +104,41 @@ k_solve_grid(DevProblem<TT> pr, DevSettings s, int kktL, GridSync gs) {
   bool ok = S.solve(g);
   __syncthreads();
   if (ok && blockIdx.x == 0 && threadIdx.x == 0) *pr.st = ssc;
+}
+
+// One thread-block cluster solves the problem (medium sizes).
+constexpr int kClusterThreads = 1024;
+template <typename TT>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+k_setup_cluster(DevProblem<TT> pr, DevSettings s, int kktL, int keep_state) {
+  namespace cgr = cooperative_groups;
+  __shared__ GroupShared gsh;
+  __shared__ SolverScalars ssc;
+  cgr::cluster_group cl = cgr::this_cluster();
+  if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (keep_state) ssc = *pr.st; }
+  __syncthreads();
+  ClusterGroup g{&gsh, cl.block_rank(), cl.num_blocks()};
+  Solver<TT> S{pr, s, &ssc, kktL};
+  if (keep_state) S.prepare_data(g, true); else S.setup(g);
+  __syncthreads();
+  if (g.rank == 0 && threadIdx.x == 0) *pr.st = ssc;
+  cl.sync();
+}
+template <typename TT>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+k_solve_cluster(DevProblem<TT> pr, DevSettings s, int kktL) {
+  namespace cgr = cooperative_groups;
+  __shared__ GroupShared gsh;
+  __shared__ SolverScalars ssc;
+  cgr::cluster_group cl = cgr::this_cluster();
+  if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; ssc = *pr.st; }
+  __syncthreads();
+  ClusterGroup g{&gsh, cl.block_rank(), cl.num_blocks()};
+  Solver<TT> S{pr, s, &ssc, kktL};
+  S.solve(g);
+  __syncthreads();
+  if (g.rank == 0 && threadIdx.x == 0) *pr.st = ssc;
+  cl.sync();
 }
 
 // Small element-wise kernels used by the update / warm-start entry points.
@@ -205,6 +241,7 @@ struct OSQPWorkspace_ {
   int kktL;
   int use_grid;
   int grid_blocks;
+  int cluster;            // >1: one thread-block cluster of this many CTAs
   unsigned int* bar;      // [count, gen]
   int* err;
   int* flag;              // scratch flag for update checks
@@ -511,11 +548,21 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   if (cudaEventCreate(&w->ev0) != cudaSuccess || cudaEventCreate(&w->ev1) != cudaSuccess) { osqp_cleanup(solver); return OSQP_ALGEBRA_LOAD_ERROR; }
 
   // Execution form: one CTA for small problems, cooperative grid otherwise.
+  // Execution form by problem size: one CTA, one thread-block cluster, or
+  // the cooperative grid.
   const long long work_nnz = (long long)nnzPf + 2LL * nnzA + n + m;
   const char* mode = getenv("OSQP_GB300_MODE");
-  w->use_grid = work_nnz > 200000;
-  if (mode && !strcmp(mode, "block")) w->use_grid = 0;
-  if (mode && !strcmp(mode, "grid")) w->use_grid = 1;
+  w->use_grid = work_nnz > 2000000;
+  w->cluster = (!w->use_grid && work_nnz > 30000) ? 16 : 1;
+  if (mode && !strcmp(mode, "block")) { w->use_grid = 0; w->cluster = 1; }
+  if (mode && !strcmp(mode, "grid")) { w->use_grid = 1; w->cluster = 1; }
+  if (mode && !strncmp(mode, "cluster", 7)) { w->use_grid = 0; w->cluster = mode[7] ? atoi(mode + 7) : 16; }
+  if (w->cluster > 1) {
+    const int c1 = max_active_clusters(k_solve_cluster<T>, w->cluster, kClusterThreads);
+    const int c2 = max_active_clusters(k_setup_cluster<T>, w->cluster, kClusterThreads);
+    if (c1 < 1 || c2 < 1) w->cluster = (w->cluster > 8 && max_active_clusters(k_solve_cluster<T>, 8, kClusterThreads) > 0 &&
+                                        max_active_clusters(k_setup_cluster<T>, 8, kClusterThreads) > 0) ? 8 : 1;
+  }
   if (w->use_grid) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_grid<T>, kGridThreads, 0);
@@ -694,6 +741,8 @@ static int launch_setup(OSQPWorkspace* w, int keep_state) {
     GridSync gs; grid_sync_args(w, gs);
     void* args[] = {(void*)&w->pr, (void*)&w->ds, (void*)&w->kktL, (void*)&keep_state, (void*)&gs};
     GB_TRY(cudaLaunchCooperativeKernel((void*)k_setup_grid<T>, dim3(w->grid_blocks), dim3(kGridThreads), args, 0, s));
+  } else if (w->cluster > 1) {
+    GB_TRY(launch_clusters(k_setup_cluster<T>, 1, w->cluster, kClusterThreads, s, w->pr, w->ds, w->kktL, keep_state));
   } else {
     k_setup_block<T><<<1, kBlockThreads, 0, s>>>(w->pr, w->ds, w->kktL, keep_state);
     GB_TRY(cudaGetLastError());
@@ -709,6 +758,8 @@ static int launch_solve(OSQPWorkspace* w) {
     GridSync gs; grid_sync_args(w, gs);
     void* args[] = {(void*)&w->pr, (void*)&w->ds, (void*)&w->kktL, (void*)&gs};
     GB_TRY(cudaLaunchCooperativeKernel((void*)k_solve_grid<T>, dim3(w->grid_blocks), dim3(kGridThreads), args, 0, s));
+  } else if (w->cluster > 1) {
+    GB_TRY(launch_clusters(k_solve_cluster<T>, 1, w->cluster, kClusterThreads, s, w->pr, w->ds, w->kktL));
   } else {
     k_solve_block<T><<<1, kBlockThreads, 0, s>>>(w->pr, w->ds, w->kktL);
     GB_TRY(cudaGetLastError());
@@ -984,7 +1035,7 @@ extern "C" OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter
   if (admm_iter) *admm_iter = w->h_st->iter;
   if (pcg_iter) *pcg_iter = w->h_st->pcg_iters_total;
   if (kernel_ms) *kernel_ms = w->last_kernel_ms;
-  if (grid_form) *grid_form = w->use_grid;
+  if (grid_form) *grid_form = w->use_grid ? 1 : (w->cluster > 1 ? w->cluster : 0);
   return 0;
 }
 

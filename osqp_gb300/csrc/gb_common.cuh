@@ -11,6 +11,7 @@
 // * CSR row kernels with 1..32 lanes per row (sub-warp per row).
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -138,6 +139,9 @@ struct GroupShared {
   double rmax[kMaxMax];
   int flag;
   int parity;   // which half of the grid partial buffers the next reduction uses
+  double csum[2][kMaxSum][2];  // cluster form: this CTA's partial sums (double-buffered)
+  double cmax[2][kMaxMax];     // cluster form: this CTA's partial maxima
+  int cidx;                    // cluster form: work item broadcast by rank 0
 };
 
 // Sum/max slot helpers shared by both group kinds.
@@ -190,6 +194,71 @@ struct BlockGroup {
     for (int i = 0; i < NS; i++) rs[i] = sh->rsum[i];
 #pragma unroll
     for (int i = 0; i < NM; i++) rm[i] = sh->rmax[i];
+    __syncthreads();
+  }
+};
+
+
+// The CTAs of one thread-block cluster cooperate on one problem: barriers are
+// the hardware cluster barrier (no spinning), and each CTA reads the other
+// CTAs' partial reductions straight from their shared memory (DSMEM) in rank
+// order, so every CTA obtains identical results.
+struct ClusterGroup {
+  GroupShared* sh;
+  unsigned rank, size;
+  __device__ int nthreads() const { return blockDim.x * size; }
+  __device__ int tid() const { return rank * blockDim.x + threadIdx.x; }
+  __device__ int nwarps() const { return (blockDim.x >> 5) * size; }
+  __device__ int warp() const { return rank * (blockDim.x >> 5) + (threadIdx.x >> 5); }
+  __device__ bool sync() { cooperative_groups::this_cluster().sync(); return true; }
+  __device__ bool ok() const { return true; }
+
+  template <typename T, int NS, int NM>
+  __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM]) {
+    namespace cgr = cooperative_groups;
+    cgr::cluster_group cl = cgr::this_cluster();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) acc_store(sh->wsum[w][i], s[i]); }
+#pragma unroll
+    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = (double)v; }
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    const int par = sh->parity;
+    if (threadIdx.x < NS) {
+      Acc<T> a;
+      for (int k = 0; k < nw; k++) a.merge(acc_load<T>(sh->wsum[k][threadIdx.x]));
+      acc_store(sh->csum[par][threadIdx.x], a);
+    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + NM) {
+      const int i = threadIdx.x - 32;
+      double a = sh->wmax[0][i];
+      for (int k = 1; k < nw; k++) a = fmax(a, sh->wmax[k][i]);
+      sh->cmax[par][i] = a;
+    }
+    cl.sync();
+    if (threadIdx.x < NS) {
+      Acc<T> a;
+      for (unsigned r = 0; r < size; r++) {
+        const double* src = cl.map_shared_rank(&sh->csum[par][threadIdx.x][0], r);
+        double t2[2] = {src[0], src[1]};
+        a.merge(acc_load<T>(t2));
+      }
+      sh->rsum[threadIdx.x] = a.value();
+    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + NM) {
+      const int i = threadIdx.x - 32;
+      double a = -INFINITY;
+      for (unsigned r = 0; r < size; r++) a = fmax(a, *cl.map_shared_rank(&sh->cmax[par][i], r));
+      sh->rmax[i] = a;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NS; i++) rs[i] = sh->rsum[i];
+#pragma unroll
+    for (int i = 0; i < NM; i++) rm[i] = sh->rmax[i];
+    __syncthreads();
+    // The other half of csum / cmax is written by the next reduction; no CTA
+    // can overwrite this half before every CTA has passed the next cluster barrier.
+    if (threadIdx.x == 0) sh->parity ^= 1;
     __syncthreads();
   }
 };

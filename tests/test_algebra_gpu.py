@@ -172,7 +172,7 @@ def test_mat_vec(alg, la):
 def test_submatrix_byrows(alg, la, case):
     L = alg.lib
     mk = lambda p: sp.csc_matrix((la[p + "/data"], la[p + "/indices"], la[p + "/indptr"]), shape=tuple(la[p + "/shape"]))
-    full = mk("test_sp_matrix_A")
+    full = mk("test_mat_vec_A")
     ind = la[f"test_submat_{case}_ind"]
     exp = mk(f"test_submat_{case}")
     M = alg.mat(full)

@@ -52,14 +52,17 @@ def check_against_oracles(oracle_lib, d, status, obj_gpu, prec):
     scale = max(1.0, abs(opt))
     err_gpu = abs(obj_gpu - opt) / scale
     err_direct = abs(rd.info["obj_val"] - opt) / scale
-    assert err_gpu <= 3.0 * err_direct + 1e-4, (err_gpu, err_direct)
+    # eps = 1e-3 accuracy class: no further from the optimum than 3x the
+    # reference's own answer, or 1e-4 (FP64) / 1e-3 (FP32) relative
+    assert err_gpu <= max(3.0 * err_direct, 1e-4 if prec == "f64" else 1e-3), (err_gpu, err_direct)
     if prec == "f64":
         # same algorithm in FP64: the GPU follows the oracle's PCG trajectory
-        assert abs(obj_gpu - ri.info["obj_val"]) / scale < 1e-6, (obj_gpu, ri.info["obj_val"])
+        assert abs(obj_gpu - ri.info["obj_val"]) / scale < 1e-5, (obj_gpu, ri.info["obj_val"])
 
 
-@pytest.mark.parametrize("prec", ["f32", "f64"])
-def test_batch_matches_oracle(prec, oracle_lib):
+@pytest.mark.parametrize("prec,cluster", [("f32", "1"), ("f64", "1"), ("f32", "8")])
+def test_batch_matches_oracle(prec, cluster, oracle_lib, monkeypatch):
+    monkeypatch.setenv("OSQP_GB300_BATCH_CLUSTER", cluster)
     lib = load(prec)
     probs = _mix(15, seed=1)
     b = Batch(lib)
@@ -72,9 +75,10 @@ def test_batch_matches_oracle(prec, oracle_lib):
         check_against_oracles(oracle_lib, d, sol["status"][k], obj_gpu, prec)
 
 
-@pytest.mark.parametrize("prec", ["f32", "f64"])
-def test_alone_and_in_mix_identical(prec):
+@pytest.mark.parametrize("prec,cluster", [("f32", "1"), ("f64", "1"), ("f32", "4")])
+def test_alone_and_in_mix_identical(prec, cluster, monkeypatch):
     """A QP gives bit-identical results solved alone or inside a batch."""
+    monkeypatch.setenv("OSQP_GB300_BATCH_CLUSTER", cluster)
     lib = load(prec)
     probs = _mix(12, seed=2)
     big = Batch(lib)

@@ -170,9 +170,9 @@ def test_portfolio_instance(prec, oracle_lib, f32, f64):
     assert_close_to_oracle(data, rg, ro, obj_rtol=1e-3, eps=1e-3, oracle_lib=oracle_lib)
 
 
-@pytest.mark.parametrize("mode", ["block", "grid"])
+@pytest.mark.parametrize("mode", ["block", "grid", "cluster4", "cluster16"])
 def test_block_and_grid_forms_agree(mode, monkeypatch, oracle_lib, f64):
-    """The one-CTA and the cooperative-grid execution forms solve the same problem."""
+    """The one-CTA, cluster and cooperative-grid execution forms solve the same problem."""
     monkeypatch.setenv("OSQP_GB300_MODE", mode)
     data = pb.random_qp(5, n=150, m=300)
     rg, _ = _solve(f64, data, INF64, **CUDA_DEFAULTS)
