@@ -133,6 +133,24 @@ OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** s, const OSQPMatrix* P, c
                                         OSQPFloat* scaled_prim_res, OSQPFloat* scaled_dual_res,
                                         OSQPInt polishing);                                   /* :46 */
 
+/* One reduced-KKT solve that allocates nothing (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc where they solve --
+ * during CUDA-graph stream capture, inside real-time loops whose memory is
+ * fixed up front -- this solves (P + sigma I + A' R A) x = b1 + A' R b2 by
+ * PCG from x = 0 (R = diag(rho_vec), or settings->rho when rho_vec is NULL;
+ * CG tolerance of the first ADMM iteration) and writes [x; A x] over b
+ * (length n + m), exactly as a freshly initialised LinSysSolver's
+ * solve(b, 1) does.  Its work vectors live in a fixed 4 MiB device array
+ * inside the library (each GPU that loads the library holds it until the
+ * process exits), so 8 n-vectors plus one m-vector, each rounded up to 256
+ * bytes, must fit in 4 MiB; larger problems return
+ * OSQP_DATA_VALIDATION_ERROR.  The first call on a device looks up that
+ * array's device address; make it before any stream capture begins.  All
+ * calls share the one array: calls that overlap on the GPU (other threads,
+ * other streams) race and must be serialised by the caller. */
+OSQPInt osqp_gb300_linsys_solve_noalloc(const OSQPMatrix* P, const OSQPMatrix* A, const OSQPVectorf* rho_vec,
+                                        const OSQPSettings* settings, OSQPVectorf* b);
+
 /* Linear-system object (include/private/types.h:243-279; layout is ABI). */
 struct linsys_solver {
   enum osqp_linsys_solver_type type;

@@ -926,3 +926,111 @@ extern "C" OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** sp, const OSQP
   *sp = &s->base;
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free reduced-KKT solve
+//
+// For callers that cannot allocate device memory at the point of the call:
+// code running while a stream is being captured into a CUDA graph, real-time
+// control loops whose memory must be fixed before the loop starts, and hosts
+// that hand the GPU to this library only through pre-sized buffers.  The PCG
+// work vectors live in the file-scope array below (kNoAllocScratchBytes per
+// device, held by every GPU that loads the library until the process exits)
+// instead of a per-solver cudaMalloc.
+// ---------------------------------------------------------------------------
+namespace gba {
+
+constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;   // 4 MiB per device
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+static void* g_noalloc_addr[64];   // device address of g_noalloc_scratch, per device
+
+// Bytes of scratch a solve with n variables and m constraints needs: eight
+// n-vectors and one m-vector, each on a 256-byte boundary.
+static size_t noalloc_bytes(long long n, long long m) {
+  auto r = [](size_t b) { return (b + 255) & ~size_t(255); };
+  return 8 * r(sizeof(T) * (size_t)(n > 0 ? n : 1)) + r(sizeof(T) * (size_t)(m > 0 ? m : 1));
+}
+
+__global__ void __launch_bounds__(kLsBlockThreads, 1)
+k_linsys_noalloc(DevProblem<T> pr, DevSettings s, int kktL, T* b, double rho) {
+  __shared__ GroupShared gsh;
+  __shared__ SolverScalars ssc;
+  if (threadIdx.x == 0) {
+    // fresh solver state: the scratch keeps whatever the previous call left
+    unsigned char* raw = reinterpret_cast<unsigned char*>(&ssc);
+    for (size_t k = 0; k < sizeof(SolverScalars); k++) raw[k] = 0;
+    ssc.rho = rho;
+    ssc.reduction_factor = s.cg_tol_fraction;
+    ssc.eps_prev = 1.0;
+    gsh.parity = 0;
+    gsh.flag = 0;
+  }
+  __syncthreads();
+  BlockGroup g{&gsh};
+  Solver<T> S{pr, s, &ssc, kktL};
+  // the iterate and search directions start at zero on every call
+  for_each(g, pr.n, [&](int i) { pr.xp[i] = T(0); pr.p0[i] = T(0); pr.p1[i] = T(0); });
+  S.update_precond(g);
+  __syncthreads();
+  S.linsys_solve(g, b, 1, false, 0.0, 0.0);
+}
+
+}  // namespace gba
+
+extern "C" OSQPInt osqp_gb300_linsys_solve_noalloc(const OSQPMatrix* P, const OSQPMatrix* A,
+                                                   const OSQPVectorf* rho_vec, const OSQPSettings* settings,
+                                                   OSQPVectorf* b) {
+  if (!P || !A || !settings || !b) return OSQP_DATA_VALIDATION_ERROR;
+  const int n = P->n, m = A->m;
+  if (b->length != n + m || A->n != n) return OSQP_DATA_VALIDATION_ERROR;
+  const size_t need = noalloc_bytes(n, m);
+  if (need > kNoAllocScratchBytes) {
+    fprintf(stderr,
+            "osqp_gb300_linsys_solve_noalloc: n=%d, m=%d needs %zu bytes of scratch; the fixed maximum is %zu bytes\n",
+            n, m, need, kNoAllocScratchBytes);
+    return OSQP_DATA_VALIDATION_ERROR;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return OSQP_ALGEBRA_LOAD_ERROR;
+  // set-up, once per device, with that device current: the host-side name of
+  // the array is not a device address, so ask the runtime for the address
+  if (!g_noalloc_addr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) {
+      fprintf(stderr, "osqp_gb300_linsys_solve_noalloc: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+      return OSQP_ALGEBRA_LOAD_ERROR;
+    }
+    g_noalloc_addr[dev] = ptr;
+  }
+  char* base = (char*)g_noalloc_addr[dev];
+  auto r = [](size_t v) { return (v + 255) & ~size_t(255); };
+  const size_t vn = r(sizeof(T) * (size_t)(n > 0 ? n : 1));
+  DevProblem<T> pr;
+  memset(&pr, 0, sizeof(pr));
+  pr.n = n; pr.m = m;
+  pr.P = P->S; pr.A = A->S; pr.At = A->At; pr.Pdiag = P->diag;
+  pr.rho_vec = rho_vec ? rho_vec->d_val : NULL;
+  pr.xp = (T*)(base + 0 * vn); pr.r = (T*)(base + 1 * vn); pr.p0 = (T*)(base + 2 * vn); pr.p1 = (T*)(base + 3 * vn);
+  pr.Kp = (T*)(base + 4 * vn); pr.yv = (T*)(base + 5 * vn); pr.rhs = (T*)(base + 6 * vn); pr.Minv = (T*)(base + 7 * vn);
+  pr.t = (T*)(base + 8 * vn);
+  DevSettings d;
+  memset(&d, 0, sizeof(d));
+  d.sigma = settings->sigma;
+  d.rho_is_vec = rho_vec ? 1 : 0;
+  d.cg_max_iter = settings->cg_max_iter;
+  d.cg_tol_reduction = settings->cg_tol_reduction;
+  d.cg_tol_fraction = settings->cg_tol_fraction;
+  d.cg_precond = (int)settings->cg_precond;
+  d.infty = (double)OSQP_INFTY;
+  const int kktL = pick_lanes((long long)P->nnzS + A->nnz, n);
+  cudaStream_t st = g_ctx.stream ? g_ctx.stream : (cudaStream_t)0;
+  k_linsys_noalloc<<<1, kLsBlockThreads, 0, st>>>(pr, d, kktL, b->d_val, (double)settings->rho);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "osqp_gb300_linsys_solve_noalloc: %s\n", cudaGetErrorString(e));
+    return OSQP_ALGEBRA_LOAD_ERROR;
+  }
+  return 0;
+}
