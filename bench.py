@@ -127,13 +127,13 @@ class ClockSampler:
 # CPU oracle arm (the reference's builtin algorithm, FP64, direct LDL^T)
 # ---------------------------------------------------------------------------
 def _cpu_worker(args):
-    lib_path, probs, lsteps, usteps = args
+    lib_path, probs, lsteps, usteps, settings = args
     from osqp_gb300.api import Library, OSQP, DIRECT_SOLVER
     lib = Library(lib_path, 64)
     solvers = []
     for (P, q, A, l, u) in probs:
         s = OSQP(lib)
-        s.setup(P, q, A, l, u, linsys_solver=DIRECT_SOLVER, **SETTINGS)
+        s.setup(P, q, A, l, u, linsys_solver=DIRECT_SOLVER, **settings)
         solvers.append(s)
     objs = []
     t0 = time.perf_counter()
@@ -162,7 +162,7 @@ def cpu_arm(probs, ls, us, sizes_m, budget_s=15.0, steps=1):
         pp = [probs[i] for i in ch]
         lst = [[ls[s][moff[i]:moff[i + 1]] for i in ch] for s in range(steps)]
         ust = [[us[s][moff[i]:moff[i + 1]] for i in ch] for s in range(steps)]
-        tasks.append((lib_path, pp, lst, ust))
+        tasks.append((lib_path, pp, lst, ust, dict(SETTINGS)))
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(len(tasks)) as pool:
@@ -312,7 +312,10 @@ def main():
     ap.add_argument("--count", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=8)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--max-iter", type=int, default=SETTINGS["max_iter"],
+                    help="ADMM iteration cap (smaller values give short profiling cases)")
     args = ap.parse_args()
+    SETTINGS["max_iter"] = args.max_iter
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     K, W = args.steps, args.warmup
