@@ -8,17 +8,29 @@
 // radix-sort transposes as the single-QP path (gb_structure.cuh), for all
 // QPs at once.
 //
-// Execution: a persistent grid of CTAs (SM count x occupancy) pulls QPs from
-// an atomic work queue ordered by decreasing nonzero count (largest first, so
-// the tail of the launch is short); each CTA runs the complete OSQP solve for
-// one QP with block-level barriers only.  No QP ever waits on another, so the
-// launch has no device-wide synchronisation at all.
+// Execution: a persistent grid pulls QPs from an atomic work queue ordered by
+// decreasing nonzero count (largest first).  Two group forms run the same
+// device solver (gb_solver.cuh):
+//   * CTA form (k_batch): one CTA per QP, block barriers only.  For a solve the
+//     CTA stages the QP's PCG vectors and row pointers (and, when they fit,
+//     its matrices) in dynamic shared memory.
+//   * cluster form (k_batch_cluster): a thread-block cluster per QP.  Each CTA
+//     owns a contiguous slice of rows, holds its slice of the matrices in
+//     shared memory and a full copy of the gathered vectors (p, A p, x~, rho),
+//     written to every CTA through distributed shared memory; reductions push
+//     per-CTA partials to every CTA and merge them in rank order.
+// A solve runs the CTA form up to a fixed ADMM iteration (the split); the QPs
+// still running then continue, from exactly where they stopped, in the
+// cluster form, so the slowest QPs no longer set the launch's makespan.  The
+// split is a fixed iteration count, so a QP's result does not depend on the
+// rest of the batch.  No QP ever waits on another.
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <numeric>
 #include <vector>
 
@@ -89,22 +101,171 @@ struct BatchArrays {
 
 enum BatchMode : int { kModeSetup = 0, kModeSolve = 1, kModeUpdateVec = 2 };
 
-// Work on one QP by a group (a CTA, or the CTAs of a cluster).
+// Shared-memory staging of one QP for a solve.
+//
+// Every CTA of the group keeps, at the same offsets, full copies of the
+// vectors that the sparse products gather (p, t = R A p, xp and the rho
+// vector): writes go to all copies (group put()).  Then, for the CTA's own
+// rows only (its Spans), the CSR row pointers, the element-wise PCG vectors
+// (r, M^-1 r, K p, M^-1, rhs) and, while they fit, the CSR entries of A, A'
+// and P.  Span-only arrays are addressed by global index through an offset
+// pointer (buffer - first index), so the solver code is unchanged.  Contents
+// that persist across ADMM iterations (xp, the rho vector, M^-1) are copied
+// in (dir > 0) and their own span back (dir < 0); the row pointers and
+// entries are copied in; the rest is scratch written before it is read.  The
+// layout is a pure function of sizes and spans, so the copy-back call
+// recomputes it.  Returns false (and changes nothing) when the gathered
+// vectors do not fit.
+template <typename TT>
+struct Stager {
+  unsigned char* base;
+  int cap, off, dir;
+  __device__ __forceinline__ unsigned* take(long long words) {
+    const long long bytes = (words * 4 + 15) & ~15LL;
+    if (words <= 0 || off + bytes > cap) return nullptr;
+    unsigned* q = (unsigned*)(base + off);
+    off += (int)bytes;
+    return q;
+  }
+  __device__ __forceinline__ static void copy(unsigned* dst, const unsigned* from, long long words) {
+    for (long long i = threadIdx.x; i < words; i += blockDim.x) dst[i] = from[i];
+  }
+  static constexpr int W = (int)(sizeof(TT) / 4);
+  // full-length copy; in: everything, back: [lo, hi)
+  __device__ __forceinline__ TT* full(TT* v, int len, int lo, int hi, bool io, bool& ok) {
+    unsigned* q = take((long long)len * W);
+    if (!q) { ok = false; return v; }
+    if (io && dir > 0) copy(q, (const unsigned*)v, (long long)len * W);
+    if (io && dir < 0) copy((unsigned*)(v + lo), (const unsigned*)((TT*)q + lo), (long long)(hi - lo) * W);
+    return (TT*)q;
+  }
+  // [lo, hi) only
+  __device__ __forceinline__ TT* span(TT* v, int lo, int hi, bool io) {
+    unsigned* q = take((long long)(hi - lo) * W);
+    if (!q) return v;
+    if (io && dir > 0) copy(q, (const unsigned*)(v + lo), (long long)(hi - lo) * W);
+    if (io && dir < 0) copy((unsigned*)(v + lo), q, (long long)(hi - lo) * W);
+    return (TT*)q - lo;
+  }
+  __device__ __forceinline__ const int* rows(const int* rowptr, int lo, int hi) {
+    unsigned* q = take(hi - lo + 1);
+    if (!q) return rowptr;
+    if (dir > 0) copy(q, (const unsigned*)(rowptr + lo), hi - lo + 1);
+    return (const int*)q - lo;
+  }
+  // entries of rows [lo, hi); rowptr holds global positions
+  __device__ __forceinline__ void entries(CSR<TT>& M, const int* grow, int lo, int hi) {
+    if (hi <= lo) return;
+    const int k0 = grow[lo], k1 = grow[hi];
+    if (k1 <= k0) return;
+    const int save = off;
+    unsigned* qc = take(k1 - k0);
+    unsigned* qv = qc ? take((long long)(k1 - k0) * W) : nullptr;
+    if (!qv) { off = save; return; }
+    if (dir > 0) {
+      copy(qc, (const unsigned*)(M.col + k0), k1 - k0);
+      copy(qv, (const unsigned*)(M.val + k0), (long long)(k1 - k0) * W);
+    }
+    M.col = (const int*)qc - k0;
+    M.val = (TT*)qv - k0;
+  }
+};
+
+template <typename TT>
+__device__ __forceinline__ bool stage_problem(DevProblem<TT>& pr, const Spans& sp, bool rho_vec,
+                                              unsigned char* base, int cap, int dir) {
+  Stager<TT> sg{base, cap, 0, dir};
+  const int n = pr.n, m = pr.m;
+  const int nlo = sp.nlo, nhi = n < sp.nhi ? n : sp.nhi;
+  const int mlo = sp.mlo, mhi = m < sp.mhi ? m : sp.mhi;
+  bool ok = true;
+  DevProblem<TT> q = pr;
+  q.p0 = sg.full(pr.p0, n, nlo, nhi, false, ok);
+  if (m) q.t = sg.full(pr.t, m, mlo, mhi, false, ok);
+  q.xp = sg.full(pr.xp, n, nlo, nhi, true, ok);
+  if (m && rho_vec) q.rho_vec = sg.full(pr.rho_vec, m, mlo, mhi, true, ok);
+  if (!ok) return false;
+  const int* growA = pr.A.rowptr;
+  const int* growAt = pr.At.rowptr;
+  const int* growP = pr.P.rowptr;
+  if (m) q.A.rowptr = sg.rows(pr.A.rowptr, mlo, mhi);
+  q.At.rowptr = sg.rows(pr.At.rowptr, nlo, nhi);
+  q.P.rowptr = sg.rows(pr.P.rowptr, nlo, nhi);
+  q.Minv = sg.span(pr.Minv, nlo, nhi, true);
+  q.r = sg.span(pr.r, nlo, nhi, false);
+  q.yv = sg.span(pr.yv, nlo, nhi, false);
+  q.Kp = sg.span(pr.Kp, nlo, nhi, false);
+  q.rhs = sg.span(pr.rhs, nlo, nhi, false);
+  if (m) sg.entries(q.A, growA, mlo, mhi);
+  sg.entries(q.At, growAt, nlo, nhi);
+  sg.entries(q.P, growP, nlo, nhi);
+  pr = q;
+  return true;
+}
+
+// Contiguous slices of a QP's rows for rank r of a c-CTA cluster, balanced by
+// estimated work: a row costs its entries plus 4 x (lanes per row), the
+// entries a sub-warp could have processed in the row's fixed per-row work.
+// n-space rows cost their P and A' entries, m-space rows their A entries.
+template <typename TT>
+__device__ Spans cluster_spans(const DevProblem<TT>& pr, int kktL, int r, int c) {
+  Spans sp;
+  auto cut = [&](const int* r1, const int* r2, int rows, long long per_row, long long target) {
+    int lo = 0, hi = rows;   // first row i with cost(i) >= target
+    const long long b1 = r1[0], b2 = r2 ? r2[0] : 0;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      const long long cst = (r1[mid] - b1) + (r2 ? (r2[mid] - b2) : 0) + per_row * mid;
+      if (cst < target) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+  };
+  const long long wn = 4LL * kktL;
+  const long long Fn = (pr.P.rowptr[pr.n] - pr.P.rowptr[0]) + (pr.At.rowptr[pr.n] - pr.At.rowptr[0]) + wn * pr.n;
+  sp.nlo = r == 0 ? 0 : cut(pr.P.rowptr, pr.At.rowptr, pr.n, wn, Fn * r / c);
+  sp.nhi = r == c - 1 ? pr.n : cut(pr.P.rowptr, pr.At.rowptr, pr.n, wn, Fn * (r + 1) / c);
+  if (pr.m) {
+    const long long wm = 4LL * pr.A.lanes;
+    const long long Fm = (pr.A.rowptr[pr.m] - pr.A.rowptr[0]) + wm * pr.m;
+    sp.mlo = r == 0 ? 0 : cut(pr.A.rowptr, nullptr, pr.m, wm, Fm * r / c);
+    sp.mhi = r == c - 1 ? pr.m : cut(pr.A.rowptr, nullptr, pr.m, wm, Fm * (r + 1) / c);
+  } else {
+    sp.mlo = 0; sp.mhi = 0;
+  }
+  return sp;
+}
+
+// Work on one QP by a group (a CTA, or the CTAs of a cluster).  `dsm` /
+// `dsm_bytes`: the CTA's dynamic shared memory for staged vectors.  A cluster
+// solving with staged vectors works on contiguous row slices per CTA.  Solves
+// run iterations it_lo..it_hi (gb_solver.cuh).
 template <typename TT, typename G>
 __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s, int k, int mode,
-                           GroupShared& gsh, SolverScalars& ssc) {
-  DevProblem<TT> pr = B.problem(k);
-  if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pr.st; }
+                           GroupShared& gsh, SolverScalars& ssc, unsigned char* dsm, int dsm_bytes,
+                           int it_lo, int it_hi) {
+  DevProblem<TT> pv = B.problem(k);
+  if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pv.st; }
   __syncthreads();
-  Solver<TT> S{pr, s, &ssc, B.inst[k].kktL};
+  bool staged = false;
+  if (mode == kModeSolve && dsm_bytes > 0) {
+    if constexpr (std::is_same<G, ClusterGroup>::value) {
+      g.sp = cluster_spans(pv, B.inst[k].kktL, (int)g.rank, (int)g.size);
+      g.sliced = true;
+    }
+    staged = stage_problem(pv, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, 1);
+    if constexpr (std::is_same<G, ClusterGroup>::value) g.repl = staged;
+    g.sync();   // staged copies complete in every CTA before any peer writes them
+  }
+  Solver<TT> S{pv, s, &ssc, B.inst[k].kktL};
   if (mode == kModeSetup) {
     S.setup(g);
   } else if (mode == kModeSolve) {
-    S.solve(g);
+    S.solve(g, it_lo, it_hi);
   } else {
     // new q / l / u from *_in with the QP's existing scaling (osqp_api.c:1184-1257)
     const TT c = (TT)ssc.c;
     const bool sc_on = s.scaling != 0;
+    const DevProblem<TT>& pr = pv;
     for_each(g, pr.n, [&](int i) { pr.q[i] = sc_on ? (pr.q_in[i] * pr.D[i]) * c : pr.q_in[i]; });
     for_each(g, pr.m, [&](int j) {
       pr.l[j] = sc_on ? pr.l_in[j] * pr.E[j] : pr.l_in[j];
@@ -119,48 +280,102 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
     if (threadIdx.x == 0) { ssc.status = ST_UNSOLVED; ssc.rho_updates = 0; }
   }
   g.sync();
+  if (staged) {
+    DevProblem<TT> pb = B.problem(k);
+    stage_problem(pb, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, -1);
+    g.sync();   // peers may still read this CTA's copies until here
+  }
+  if constexpr (std::is_same<G, ClusterGroup>::value) {
+    g.sp = Spans{};
+    g.sliced = false;
+    g.repl = false;
+  }
 }
 
-// Persistent kernel, one CTA per QP: CTAs pull QPs from the queue.
-template <typename TT>
-__global__ void __launch_bounds__(kBatchThreads, 2)
-k_batch(BatchArrays<TT> B, DevSettings s, int count, int* queue, const int* order, int mode) {
+// Batch launch parameters shared by both kernels.  The queue holds `count`
+// entries of `order`, or *count_dev entries when count_dev is set (a list
+// built on the device by an earlier launch of the same stream).
+struct BatchLaunch {
+  int count;
+  const int* count_dev;
+  int* queue;
+  const int* order;
+  int mode;
+  int it_lo, it_hi;   // solve window
+  int dsm_bytes;      // CTA form: dynamic shared memory for staged vectors
+};
+
+extern __shared__ __align__(16) unsigned char g_batch_dsm[];
+
+// Persistent kernel, one CTA per QP: CTAs pull QPs from the queue.  NT
+// threads per CTA, MINB CTAs per SM.
+template <typename TT, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+k_batch(BatchArrays<TT> B, DevSettings s, BatchLaunch L) {
   __shared__ GroupShared gsh;
   __shared__ SolverScalars ssc;
   __shared__ int s_idx;
   BlockGroup g{&gsh};
+  const int count = L.count_dev ? *L.count_dev : L.count;
   for (;;) {
-    if (threadIdx.x == 0) s_idx = atomicAdd(queue, 1);
+    if (threadIdx.x == 0) s_idx = atomicAdd(L.queue, 1);
     __syncthreads();
     const int idx = s_idx;
     __syncthreads();
     if (idx >= count) break;
-    batch_item(g, B, s, order[idx], mode, gsh, ssc);
-    if (threadIdx.x == 0) *B.problem(order[idx]).st = ssc;
+    batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi);
+    if (threadIdx.x == 0) *B.problem(L.order[idx]).st = ssc;
     __syncthreads();
   }
 }
 
 // Persistent kernel, one thread-block cluster per QP: the cluster's rank-0 CTA
 // pulls a QP and broadcasts it through distributed shared memory.
-template <typename TT>
-__global__ void __launch_bounds__(kBatchThreads, 1)
-k_batch_cluster(BatchArrays<TT> B, DevSettings s, int count, int* queue, const int* order, int mode) {
+template <typename TT, int NT>
+__global__ void __launch_bounds__(NT, 1)
+k_batch_cluster(BatchArrays<TT> B, DevSettings s, BatchLaunch L) {
   namespace cgr = cooperative_groups;
   __shared__ GroupShared gsh;
   __shared__ SolverScalars ssc;
   cgr::cluster_group cl = cgr::this_cluster();
   ClusterGroup g{&gsh, cl.block_rank(), cl.num_blocks()};
+  const int count = L.count_dev ? *L.count_dev : L.count;
   for (;;) {
-    if (g.rank == 0 && threadIdx.x == 0) gsh.cidx = atomicAdd(queue, 1);
+    if (g.rank == 0 && threadIdx.x == 0) gsh.cidx = atomicAdd(L.queue, 1);
     cl.sync();
     const int idx = *cl.map_shared_rank(&gsh.cidx, 0);
     cl.sync();   // rank 0 keeps its shared memory until every CTA has read idx
     if (idx >= count) break;
-    batch_item(g, B, s, order[idx], mode, gsh, ssc);
-    if (g.rank == 0 && threadIdx.x == 0) *B.problem(order[idx]).st = ssc;
+    batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi);
+    if (g.rank == 0 && threadIdx.x == 0) *B.problem(L.order[idx]).st = ssc;
     cl.sync();
   }
+}
+
+// The QPs of `order` whose solve is suspended (status still ST_UNSOLVED after
+// a windowed launch), in queue order, and their count.  One CTA.
+__global__ void k_batch_unfinished(const SolverScalars* st, const int* order, int count, int* order2,
+                                   int* count2) {
+  __shared__ int wtot[32];
+  __shared__ int base;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < count; c0 += blockDim.x) {
+    const int i = c0 + threadIdx.x;
+    const int k = i < count ? order[i] : -1;
+    const bool f = k >= 0 && st[k].status == ST_UNSOLVED;
+    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) wtot[w] = __popc(bal);
+    __syncthreads();
+    int off = base;
+    for (int q = 0; q < w; q++) off += wtot[q];
+    if (f) order2[off + __popc(bal & ((1u << lane) - 1u))] = k;
+    __syncthreads();
+    if (threadIdx.x == 0) { int t = 0; for (int q = 0; q < nw; q++) t += wtot[q]; base += t; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count2 = base;
 }
 
 // ---- structure kernels (one CTA per QP) ----
@@ -257,6 +472,50 @@ __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out,
 
 using namespace gbb;
 
+typedef void (*BatchKernel)(BatchArrays<T>, DevSettings, BatchLaunch);
+
+// The CTA form's kernel for a CTA size (512 threads x 2 per SM, or 1024 x 1).
+static void cta_form(int threads, BatchKernel* fn, int* nt, int* minb) {
+  if (threads >= 1024) { *fn = k_batch<T, 1024, 1>; *nt = 1024; *minb = 1; }
+  else { *fn = k_batch<T, kBatchThreads, 2>; *nt = kBatchThreads; *minb = 2; }
+}
+// The cluster form's kernel for a CTA size (one CTA per SM).
+static void cluster_form(int threads, BatchKernel* fn, int* nt) {
+  if (threads >= 1024) { *fn = k_batch_cluster<T, 1024>; *nt = 1024; }
+  else { *fn = k_batch_cluster<T, kBatchThreads>; *nt = kBatchThreads; }
+}
+
+// Largest dynamic shared memory per CTA (whole KiB, at most cap_bytes) that
+// keeps minb CTAs of the kernel resident per SM; 0 if none.
+static int configure_dsm(BatchKernel fn, int threads, int minb, int device, long cap_bytes) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return 0;
+  int smem_sm = 0, reserved = 0, optin = 0;
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, device);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  long per_cta = (long)smem_sm / minb - reserved - (long)fa.sharedSizeBytes;
+  per_cta = std::min(per_cta, (long)optin - (long)fa.sharedSizeBytes);
+  if (cap_bytes >= 0) per_cta = std::min(per_cta, cap_bytes);
+  per_cta &= ~1023L;
+  while (per_cta > 0) {
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)per_cta) == cudaSuccess) {
+      int nb = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, (size_t)per_cta) == cudaSuccess &&
+          nb >= minb)
+        break;
+    }
+    per_cta -= 1024;
+  }
+  cudaGetLastError();
+  return (int)std::max(per_cta, 0L);
+}
+
+static int env_int(const char* name, int dflt) {
+  const char* e = getenv(name);
+  return (e && *e) ? atoi(e) : dflt;
+}
+
 struct OSQPBatch_ {
   int count, device;
   long long nsum, msum, nnzT, nnzA, nnzPf;
@@ -275,7 +534,15 @@ struct OSQPBatch_ {
   DevSettings ds;
   OSQPSettings settings;
   int grid;
-  int cluster;   // CTAs per QP (1 = one CTA per QP)
+  int cluster;   // 0: one CTA per QP (k_batch); c >= 1: clusters of c CTAs per QP
+  BatchKernel kfn;        // CTA form: k_batch instantiation
+  int threads;            // CTA form: threads per CTA
+  int dsm;                // CTA form: dynamic shared memory per CTA for staged vectors (solves)
+  BatchKernel cfn;        // cluster forms (main and tail): k_batch_cluster instantiation
+  int cthreads, cdsm;     // cluster forms: threads and dynamic shared memory per CTA
+  int split;              // ADMM iteration after which unfinished QPs move to the tail form (0: never)
+  int tail_cluster, tail_grid;   // tail form: CTAs per QP and resident clusters
+  int *d_order2, *d_count2, *d_queue2;
   float last_ms, last_step_ms;
   long long last_admm, last_pcg;
   std::vector<BatchInst> inst;
@@ -305,12 +572,33 @@ static DevSettings batch_dev_settings(const OSQPSettings* st) {
 
 static int run_batch_kernel(OSQPBatch* b, int mode) {
   BT_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream));
-  if (b->cluster > 1) {
-    BT_TRY(launch_clusters(k_batch_cluster<T>, b->grid, b->cluster, kBatchThreads, b->stream,
-                           b->B, b->ds, b->count, b->d_queue, (const int*)b->d_order, mode));
+  BatchLaunch L{b->count, nullptr, b->d_queue, b->d_order, mode, 1, 0x7fffffff, 0};
+  const bool split = mode == kModeSolve && b->split > 0 && b->split < b->ds.max_iter && b->cluster < b->tail_cluster;
+  if (split) L.it_hi = b->split;
+  if (b->cluster >= 1) {
+    L.dsm_bytes = mode == kModeSolve ? b->cdsm : 0;
+    BT_TRY(launch_clusters_dsm(b->cfn, b->grid, b->cluster, b->cthreads, (size_t)b->cdsm, b->stream, b->B, b->ds, L));
   } else {
-    k_batch<T><<<b->grid, kBatchThreads, 0, b->stream>>>(b->B, b->ds, b->count, b->d_queue, b->d_order, mode);
+    L.dsm_bytes = mode == kModeSolve ? b->dsm : 0;
+    b->kfn<<<b->grid, b->threads, (size_t)L.dsm_bytes, b->stream>>>(b->B, b->ds, L);
     BT_TRY(cudaGetLastError());
+  }
+  if (split) {
+    // QPs still running after `split` iterations continue, from where they
+    // stopped, with a cluster of CTAs each: the slowest QPs set the makespan
+    k_batch_unfinished<<<1, 1024, 0, b->stream>>>(b->B.st, b->d_order, b->count, b->d_order2, b->d_count2);
+    BT_TRY(cudaGetLastError());
+    BT_TRY(cudaMemsetAsync(b->d_queue2, 0, sizeof(int), b->stream));
+    BatchLaunch T2{0, b->d_count2, b->d_queue2, b->d_order2, kModeSolve, b->split + 1, 0x7fffffff, 0};
+    if (b->tail_cluster >= 1) {
+      T2.dsm_bytes = b->cdsm;
+      BT_TRY(launch_clusters_dsm(b->cfn, b->tail_grid, b->tail_cluster, b->cthreads, (size_t)b->cdsm, b->stream,
+                                 b->B, b->ds, T2));
+    } else {
+      T2.dsm_bytes = b->dsm;
+      b->kfn<<<b->grid, b->threads, (size_t)b->dsm, b->stream>>>(b->B, b->ds, T2);
+      BT_TRY(cudaGetLastError());
+    }
   }
   return 0;
 }
@@ -430,6 +718,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   for (int k = 0; k < 16; k++) o_vm[k] = pl.take(sizeof(T) * msum);
   size_t o_ctype = pl.take(sizeof(int) * msum), o_st = pl.take(sizeof(SolverScalars) * count);
   size_t o_inst = pl.take(sizeof(BatchInst) * count), o_order = pl.take(sizeof(int) * count);
+  size_t o_order2 = pl.take(sizeof(int) * count);
   size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 2);
   size_t o_sq = pl.take(sizeof(T) * nsum), o_sl = pl.take(sizeof(T) * msum), o_su = pl.take(sizeof(T) * msum);
   if (cudaMalloc(&b->arena, pl.off) != cudaSuccess) { osqp_gb300_batch_cleanup(b); return OSQP_MEM_ALLOC_ERROR; }
@@ -447,6 +736,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   b->d_inst = (BatchInst*)(a + o_inst); B.inst = b->d_inst;
   b->d_order = (int*)(a + o_order);
   b->d_queue = (int*)(a + o_misc); b->d_flag = b->d_queue + 1;
+  b->d_queue2 = b->d_queue + 2; b->d_count2 = b->d_queue + 3; b->d_order2 = (int*)(a + o_order2);
   b->d_info = (BatchInfo*)(a + o_info); b->d_totals = (long long*)(a + o_tot);
   b->stage_q = (T*)(a + o_sq); b->stage_l = (T*)(a + o_sl); b->stage_u = (T*)(a + o_su);
 
@@ -518,17 +808,37 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   // ---- persistent grid: SMs x resident CTAs, or resident clusters ----
   int per_sm = 0, sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-  const char* cenv = getenv("OSQP_GB300_BATCH_CLUSTER");
-  b->cluster = cenv ? std::max(1, std::min(16, atoi(cenv))) : 1;
-  if (b->cluster > 1) {
-    int nclusters = max_active_clusters(k_batch_cluster<T>, b->cluster, kBatchThreads);
-    if (nclusters < 1) b->cluster = 1;
+  const int cap_kib = env_int("OSQP_GB300_BATCH_SMEM_KIB", -1);
+  const long cap = cap_kib < 0 ? -1L : 1024L * cap_kib;
+  cluster_form(env_int("OSQP_GB300_BATCH_CLUSTER_THREADS", 1024), &b->cfn, &b->cthreads);
+  b->cdsm = configure_dsm(b->cfn, b->cthreads, 1, b->device, cap);
+  // OSQP_GB300_BATCH_CLUSTER: 0 = one CTA per QP (k_batch), c >= 1 = clusters
+  // of c CTAs per QP (k_batch_cluster, sliced rows, replicated vectors)
+  b->cluster = std::max(0, std::min(16, env_int("OSQP_GB300_BATCH_CLUSTER", 0)));
+  if (b->cluster >= 1) {
+    int nclusters = max_active_clusters(b->cfn, b->cluster, b->cthreads, (size_t)b->cdsm);
+    if (nclusters < 1) b->cluster = 0;
     else b->grid = std::max(1, std::min(count, nclusters));   // grid counted in clusters
   }
-  if (b->cluster <= 1) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<T>, kBatchThreads, 0);
+  int minb = 2;
+  cta_form(env_int("OSQP_GB300_BATCH_THREADS", 1024), &b->kfn, &b->threads, &minb);
+  b->dsm = configure_dsm(b->kfn, b->threads, minb, b->device, cap);
+  if (b->cluster == 0) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->kfn, b->threads, (size_t)b->dsm);
     b->grid = std::max(1, std::min(count, sms * std::max(per_sm, 1)));
   }
+  // Defaults measured on 4096 batched MPC QPs (GB300): one 1024-thread CTA
+  // per QP with staged vectors, and QPs still running after 1000 ADMM
+  // iterations continue on 8-CTA clusters with the QP in shared memory.
+  b->split = std::max(0, env_int("OSQP_GB300_BATCH_SPLIT", 1000));
+  b->tail_cluster = std::max(0, std::min(16, env_int("OSQP_GB300_BATCH_TAIL", 8)));
+  b->tail_grid = 0;
+  while (b->split > 0 && b->tail_cluster >= 1) {
+    b->tail_grid = max_active_clusters(b->cfn, b->tail_cluster, b->cthreads, (size_t)b->cdsm);
+    if (b->tail_grid >= 1) break;
+    b->tail_cluster /= 2;
+  }
+  cudaGetLastError();
 
   int rc = run_batch_kernel(b, kModeSetup);
   if (rc) { osqp_gb300_batch_cleanup(b); return rc; }

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace gb {
 
 constexpr int kMaxSum = 8;   // FP64 sum slots per reduction
@@ -111,6 +113,9 @@ template <> struct Acc<double> {
 };
 
 template <typename T>
+__device__ __forceinline__ T tmaxT(T a, T b) { return a > b ? a : (b == b ? b : a); }
+
+template <typename T>
 __device__ __forceinline__ T warp_maxT(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -132,16 +137,36 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // Groups
 // ---------------------------------------------------------------------------
 // Shared scratch every group needs: per-warp partials and broadcast results.
+constexpr int kMaxRanks = 16;   // CTAs per cluster
+
 struct GroupShared {
-  double wsum[32][kMaxSum][2];   // per-warp partial sums (hi, lo) or (v, 0)
-  double wmax[32][kMaxMax];      // per-warp partial maxima
+  // per-warp partials, one 64-bit word each in the iterate type's own bits
+  // (acc_pack / max_pack: no FP64 conversion on the way)
+  double wsum[32][kMaxSum];
+  double wmax[32][kMaxMax];
   double rsum[kMaxSum];
   double rmax[kMaxMax];
   int flag;
-  int parity;   // which half of the grid partial buffers the next reduction uses
-  double csum[2][kMaxSum][2];  // cluster form: this CTA's partial sums (double-buffered)
-  double cmax[2][kMaxMax];     // cluster form: this CTA's partial maxima
+  int parity;   // which half of the double-buffered partials the next reduction uses
+  // cluster form: every CTA's per-CTA partials, pushed by their owners
+  // (sum slots packed as one 64-bit word, then max slots)
+  double recv[2][kMaxRanks][kMaxSum + kMaxMax];
   int cidx;                    // cluster form: work item broadcast by rank 0
+  // scalars computed once per reduction by one thread and broadcast
+  double bd[4];    // FP64 state
+  double bdT[4];   // values of the iterate type (FP64 build)
+  float bf[4];     // values of the iterate type (FP32 build)
+  int bi[4];
+};
+
+// Broadcast slots of the iterate type T.
+template <typename T> __device__ __forceinline__ T* bcast_slots(GroupShared* sh);
+template <> __device__ __forceinline__ float* bcast_slots<float>(GroupShared* sh) { return sh->bf; }
+template <> __device__ __forceinline__ double* bcast_slots<double>(GroupShared* sh) { return sh->bdT; }
+
+// Reduction callback placeholder: no scalar follow-up.
+struct NoFn {
+  __device__ void operator()(const double*, const double*) const {}
 };
 
 // Sum/max slot helpers shared by both group kinds.
@@ -158,43 +183,129 @@ __device__ __forceinline__ Acc<float> acc_load<float>(const double* src) { Acc<f
 template <>
 __device__ __forceinline__ Acc<double> acc_load<double>(const double* src) { Acc<double> a; a.v = src[0]; return a; }
 
+// The part of a problem's index spaces a CTA works on: rows / entries
+// [nlo, nhi) of the n-space (x, P, A') and [mlo, mhi) of the m-space (z, A).
+// The defaults cover everything; a sliced cluster narrows them per CTA.
+struct Spans {
+  int nlo = 0, nhi = 0x7fffffff, mlo = 0, mhi = 0x7fffffff;
+};
+struct Rng { int lo, hi; };
+
+// A sum slot packed into one 64-bit word (FP32 build: the two floats).
+template <typename T> __device__ __forceinline__ double acc_pack(const Acc<T>& a);
+template <> __device__ __forceinline__ double acc_pack<float>(const Acc<float>& a) {
+  return __hiloint2double(__float_as_int(a.hi), __float_as_int(a.lo));
+}
+template <> __device__ __forceinline__ double acc_pack<double>(const Acc<double>& a) { return a.v; }
+template <typename T> __device__ __forceinline__ Acc<T> acc_unpack(double w);
+template <> __device__ __forceinline__ Acc<float> acc_unpack<float>(double w) {
+  Acc<float> a; a.hi = __int_as_float(__double2hiint(w)); a.lo = __int_as_float(__double2loint(w)); return a;
+}
+template <> __device__ __forceinline__ Acc<double> acc_unpack<double>(double w) { Acc<double> a; a.v = w; return a; }
+template <typename T> __device__ __forceinline__ double max_pack(T v);
+template <> __device__ __forceinline__ double max_pack<float>(float v) { return __hiloint2double(0, __float_as_int(v)); }
+template <> __device__ __forceinline__ double max_pack<double>(double v) { return v; }
+template <typename T> __device__ __forceinline__ T max_unpack(double w);
+template <> __device__ __forceinline__ float max_unpack<float>(double w) { return __int_as_float(__double2loint(w)); }
+template <> __device__ __forceinline__ double max_unpack<double>(double w) { return w; }
+
+// Slot `slot` of the per-warp partials reduced across the CTA's warps by the
+// calling warp (lane k holds warp k's partial; fixed shuffle order).  Sum
+// slots (slot < NS) return the packed Acc, max slots the maximum.
+template <typename T, int NS>
+__device__ __forceinline__ double cta_slot(GroupShared* sh, int slot) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (slot < NS) {
+    Acc<T> a;
+    if (lane < nw) a = acc_unpack<T>(sh->wsum[lane][slot]);
+    warp_accT(a);
+    return acc_pack<T>(a);
+  }
+  T a = lane < nw ? max_unpack<T>(sh->wmax[lane][slot - NS]) : T(-INFINITY);
+  return max_pack<T>(warp_maxT(a));
+}
+
+// Per-warp partials of a CTA -> per-CTA values: sum slot i is reduced by
+// warp i (lane k holds warp k's partial; fixed shuffle order), max slots by
+// the following warps.  Sums go out as (hi, lo) pairs when sum2 is set, else
+// as FP64 values in sumv.  At most 32 warps.
+template <typename T, int NS, int NM>
+__device__ __forceinline__ void cta_finish(GroupShared* sh, double (*sum2)[2], double* sumv, double* maxv) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int slot = w; slot < NS + NM; slot += nw) {
+    if (slot < NS) {
+      Acc<T> a;
+      if (lane < nw) a = acc_unpack<T>(sh->wsum[lane][slot]);
+      warp_accT(a);
+      if (lane == 0) {
+        if (sum2) acc_store(sum2[slot], a);
+        else sumv[slot] = a.value();
+      }
+    } else {
+      const int i = slot - NS;
+      T a = lane < nw ? max_unpack<T>(sh->wmax[lane][i]) : T(-INFINITY);
+      a = warp_maxT(a);
+      if (lane == 0) maxv[i] = (double)a;
+    }
+  }
+}
+
 // One CTA cooperates on one problem.
 struct BlockGroup {
   GroupShared* sh;
+  Spans sp;
   __device__ int nthreads() const { return blockDim.x; }
   __device__ int tid() const { return threadIdx.x; }
   __device__ int nwarps() const { return blockDim.x >> 5; }
   __device__ int warp() const { return threadIdx.x >> 5; }
+  // span iteration: first thread / warp and stride
+  __device__ int t0() const { return threadIdx.x; }
+  __device__ int ts() const { return blockDim.x; }
+  __device__ int w0() const { return threadIdx.x >> 5; }
+  __device__ int ws() const { return blockDim.x >> 5; }
+  template <typename T> __device__ void put(T* v, int i, T val) const { v[i] = val; }
   __device__ bool sync() { __syncthreads(); return true; }
   __device__ bool ok() const { return true; }
 
   // Reduce NS sums and NM maxima across the CTA; every thread receives the
-  // FP64 results in rs / rm.
-  template <typename T, int NS, int NM>
-  __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM]) {
+  // FP64 results in rs / rm.  fn(rsum, rmax), if given, runs once (thread 0)
+  // on the results before they are published, for scalar follow-up math
+  // whose outputs go to shared memory (bd / bf / bi).
+  template <typename T, int NS, int NM, typename FN = NoFn>
+  __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM], FN fn = FN()) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) acc_store(sh->wsum[w][i], s[i]); }
+    for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) sh->wsum[w][i] = acc_pack<T>(s[i]); }
 #pragma unroll
-    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = (double)v; }
+    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
     __syncthreads();
-    const int nw = blockDim.x >> 5;
-    if (threadIdx.x < NS) {
-      Acc<T> a;
-      for (int k = 0; k < nw; k++) a.merge(acc_load<T>(sh->wsum[k][threadIdx.x]));
-      sh->rsum[threadIdx.x] = a.value();
-    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + NM) {
-      const int i = threadIdx.x - 32;
-      double a = sh->wmax[0][i];
-      for (int k = 1; k < nw; k++) a = fmax(a, sh->wmax[k][i]);
-      sh->rmax[i] = a;
+    if constexpr (NS + NM <= 4) {
+      // small reductions: warp 0 finishes every slot, lane 0 runs fn
+      if (w == 0) {
+#pragma unroll
+        for (int slot = 0; slot < NS + NM; slot++) {
+          const double v = cta_slot<T, NS>(sh, slot);
+          if (lane == 0) {
+            if (slot < NS) sh->rsum[slot] = acc_unpack<T>(v).value();
+            else sh->rmax[slot - NS] = (double)max_unpack<T>(v);
+          }
+        }
+        if (lane == 0) fn(sh->rsum, sh->rmax);
+      }
+    } else {
+      cta_finish<T, NS, NM>(sh, nullptr, sh->rsum, sh->rmax);
+      if constexpr (!std::is_same<FN, NoFn>::value) {
+        __syncthreads();
+        if (threadIdx.x == 0) fn(sh->rsum, sh->rmax);
+      }
     }
     __syncthreads();
+    // rsum / rmax / bd / bf / bi are rewritten only after the next
+    // reduction's first barrier, which every thread reaches after reading them.
 #pragma unroll
     for (int i = 0; i < NS; i++) rs[i] = sh->rsum[i];
 #pragma unroll
     for (int i = 0; i < NM; i++) rm[i] = sh->rmax[i];
-    __syncthreads();
   }
 };
 
@@ -206,60 +317,82 @@ struct BlockGroup {
 struct ClusterGroup {
   GroupShared* sh;
   unsigned rank, size;
+  Spans sp;
+  bool sliced = false;   // spans are this CTA's own contiguous slices
+  bool repl = false;     // put() writes every CTA's copy (replicated shared-memory vectors)
   __device__ int nthreads() const { return blockDim.x * size; }
   __device__ int tid() const { return rank * blockDim.x + threadIdx.x; }
   __device__ int nwarps() const { return (blockDim.x >> 5) * size; }
   __device__ int warp() const { return rank * (blockDim.x >> 5) + (threadIdx.x >> 5); }
+  __device__ int t0() const { return sliced ? (int)threadIdx.x : tid(); }
+  __device__ int ts() const { return sliced ? (int)blockDim.x : nthreads(); }
+  __device__ int w0() const { return sliced ? (int)(threadIdx.x >> 5) : warp(); }
+  __device__ int ws() const { return sliced ? (int)(blockDim.x >> 5) : nwarps(); }
+  // Store v[i] = val; with replicated vectors every CTA of the cluster holds
+  // a copy of v at the same shared-memory offset, and all copies are written.
+  template <typename T> __device__ void put(T* v, int i, T val) const {
+    if (!repl) { v[i] = val; return; }
+    namespace cgr = cooperative_groups;
+    cgr::cluster_group cl = cgr::this_cluster();
+    for (unsigned r = 0; r < size; r++) *cl.map_shared_rank(v + i, r) = val;
+  }
   __device__ bool sync() { cooperative_groups::this_cluster().sync(); return true; }
   __device__ bool ok() const { return true; }
 
-  template <typename T, int NS, int NM>
-  __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM]) {
+  // Cluster reduction: each CTA reduces its warps (warp 0), pushes its
+  // per-CTA partials into every CTA's `recv` (DSMEM stores), then after one
+  // cluster barrier every CTA merges the ranks' partials in rank order from
+  // its own shared memory, so all CTAs obtain identical values.
+  template <typename T, int NS, int NM, typename FN = NoFn>
+  __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM], FN fn = FN()) {
     namespace cgr = cooperative_groups;
     cgr::cluster_group cl = cgr::this_cluster();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int NSL = NS + NM;
 #pragma unroll
-    for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) acc_store(sh->wsum[w][i], s[i]); }
+    for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) sh->wsum[w][i] = acc_pack<T>(s[i]); }
 #pragma unroll
-    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = (double)v; }
+    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
     __syncthreads();
-    const int nw = blockDim.x >> 5;
     const int par = sh->parity;
-    if (threadIdx.x < NS) {
-      Acc<T> a;
-      for (int k = 0; k < nw; k++) a.merge(acc_load<T>(sh->wsum[k][threadIdx.x]));
-      acc_store(sh->csum[par][threadIdx.x], a);
-    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + NM) {
-      const int i = threadIdx.x - 32;
-      double a = sh->wmax[0][i];
-      for (int k = 1; k < nw; k++) a = fmax(a, sh->wmax[k][i]);
-      sh->cmax[par][i] = a;
+    if (w == 0) {
+      // every lane ends with each slot's value (xor-butterfly reductions)
+#pragma unroll
+      for (int slot = 0; slot < NSL; slot++) {
+        const double v = cta_slot<T, NS>(sh, slot);
+        if (lane == slot) sh->recv[par][rank][slot] = v;
+      }
+      __syncwarp();
+      // push this CTA's partials to the other ranks: lane handles (slot, rank) pairs
+      for (int q = lane; q < NSL * (int)size; q += 32) {
+        const int slot = q % NSL, r = q / NSL;
+        if (r != (int)rank) *cl.map_shared_rank(&sh->recv[par][rank][slot], (unsigned)r) = sh->recv[par][rank][slot];
+      }
     }
     cl.sync();
-    if (threadIdx.x < NS) {
-      Acc<T> a;
-      for (unsigned r = 0; r < size; r++) {
-        const double* src = cl.map_shared_rank(&sh->csum[par][threadIdx.x][0], r);
-        double t2[2] = {src[0], src[1]};
-        a.merge(acc_load<T>(t2));
+    if (w == 0) {
+      if (lane < NS) {
+        Acc<T> a;
+        for (unsigned r = 0; r < size; r++) a.merge(acc_unpack<T>(sh->recv[par][r][lane]));
+        sh->rsum[lane] = a.value();
+      } else if (lane < NSL) {
+        T a = T(-INFINITY);
+        for (unsigned r = 0; r < size; r++) a = tmaxT(a, max_unpack<T>(sh->recv[par][r][lane]));
+        sh->rmax[lane - NS] = (double)a;
       }
-      sh->rsum[threadIdx.x] = a.value();
-    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + NM) {
-      const int i = threadIdx.x - 32;
-      double a = -INFINITY;
-      for (unsigned r = 0; r < size; r++) a = fmax(a, *cl.map_shared_rank(&sh->cmax[par][i], r));
-      sh->rmax[i] = a;
+      __syncwarp();
+      if (lane == 0) fn(sh->rsum, sh->rmax);
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < NS; i++) rs[i] = sh->rsum[i];
 #pragma unroll
     for (int i = 0; i < NM; i++) rm[i] = sh->rmax[i];
-    __syncthreads();
-    // The other half of csum / cmax is written by the next reduction; no CTA
-    // can overwrite this half before every CTA has passed the next cluster barrier.
+    // The other half of recv is written by the next reduction; no CTA can
+    // overwrite this half before every CTA has passed the next cluster
+    // barrier.  rsum / rmax are rewritten only after the next reduction's
+    // first block barrier, which every thread reaches after reading them.
     if (threadIdx.x == 0) sh->parity ^= 1;
-    __syncthreads();
   }
 };
 
@@ -275,10 +408,16 @@ struct GridSync {
 struct GridGroup {
   GroupShared* sh;
   GridSync gs;
+  Spans sp;
   __device__ int nthreads() const { return blockDim.x * gridDim.x; }
   __device__ int tid() const { return blockIdx.x * blockDim.x + threadIdx.x; }
   __device__ int nwarps() const { return (blockDim.x >> 5) * gridDim.x; }
   __device__ int warp() const { return blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); }
+  __device__ int t0() const { return tid(); }
+  __device__ int ts() const { return nthreads(); }
+  __device__ int w0() const { return warp(); }
+  __device__ int ws() const { return nwarps(); }
+  template <typename T> __device__ void put(T* v, int i, T val) const { v[i] = val; }
 
   // Bounded barrier.  Returns false (in every CTA) once any CTA timed out.
   __device__ bool sync() {
@@ -308,13 +447,13 @@ struct GridGroup {
   }
   __device__ bool ok() const { return sh->flag == 0; }
 
-  template <typename T, int NS, int NM>
-  __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM]) {
+  template <typename T, int NS, int NM, typename FN = NoFn>
+  __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM], FN fn = FN()) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) acc_store(sh->wsum[w][i], s[i]); }
+    for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) sh->wsum[w][i] = acc_pack<T>(s[i]); }
 #pragma unroll
-    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = (double)v; }
+    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
     __syncthreads();
     const int nw = blockDim.x >> 5, nb = gridDim.x;
     const int par = sh->parity;
@@ -322,12 +461,13 @@ struct GridGroup {
     double* pm = gs.partial_max + (size_t)par * kMaxMax * nb;       // [slot][block]
     if (threadIdx.x < NS) {
       Acc<T> a;
-      for (int k = 0; k < nw; k++) a.merge(acc_load<T>(sh->wsum[k][threadIdx.x]));
+      for (int k = 0; k < nw; k++) a.merge(acc_unpack<T>(sh->wsum[k][threadIdx.x]));
       acc_store(ps + ((size_t)threadIdx.x * nb + blockIdx.x) * 2, a);
     } else if (threadIdx.x >= 32 && threadIdx.x < 32 + NM) {
       const int i = threadIdx.x - 32;
-      double a = sh->wmax[0][i];
-      for (int k = 1; k < nw; k++) a = fmax(a, sh->wmax[k][i]);
+      T at = max_unpack<T>(sh->wmax[0][i]);
+      for (int k = 1; k < nw; k++) at = tmaxT(at, max_unpack<T>(sh->wmax[k][i]));
+      const double a = (double)at;
       pm[i * nb + blockIdx.x] = a;
     }
     sync();
@@ -352,6 +492,10 @@ struct GridGroup {
         a = warp_max(a);
         if (lane == 0) sh->rmax[i] = a;
       }
+    }
+    if constexpr (!std::is_same<FN, NoFn>::value) {
+      __syncthreads();
+      if (threadIdx.x == 0) fn(sh->rsum, sh->rmax);
     }
     __syncthreads();
 #pragma unroll
@@ -381,24 +525,31 @@ struct CSR {
 // Dot product of one CSR row segment handled by a sub-warp lane: entries
 // b+sl, b+sl+L, ... < e.  Four entries are fetched per round before any is
 // used, so each lane keeps four index/value loads and four gathers in flight.
+// Entries per lane loaded before any is used: the index/value loads of a
+// chunk are independent, so a row costs ceil(len / (kRowUnroll * L)) memory
+// latencies.  The summation order (k ascending per lane) does not depend on
+// it.  (8 measured slower than 4 on batched MPC: more predicated work on the
+// many short rows.)
+constexpr int kRowUnroll = 4;
+
 template <int L, typename T, typename XF>
 __device__ __forceinline__ T lane_row_dot(const int* __restrict__ col, const T* __restrict__ val,
                                           int b, int e, int sl, XF xf) {
   T acc = T(0);
-  for (int k0 = b + sl; k0 < e; k0 += 4 * L) {
-    int c[4];
-    T v[4];
+  for (int k0 = b + sl; k0 < e; k0 += kRowUnroll * L) {
+    int c[kRowUnroll];
+    T v[kRowUnroll];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (int u = 0; u < kRowUnroll; u++) {
       const int k = k0 + u * L;
       c[u] = k < e ? col[k] : -1;
       v[u] = k < e ? val[k] : T(0);
     }
-    T x[4];
+    T x[kRowUnroll];
 #pragma unroll
-    for (int u = 0; u < 4; u++) x[u] = c[u] >= 0 ? xf(c[u]) : T(0);
+    for (int u = 0; u < kRowUnroll; u++) x[u] = c[u] >= 0 ? xf(c[u]) : T(0);
 #pragma unroll
-    for (int u = 0; u < 4; u++) acc += v[u] * x[u];
+    for (int u = 0; u < kRowUnroll; u++) acc += v[u] * x[u];
   }
   return acc;
 }
@@ -493,6 +644,74 @@ inline int pick_lanes(long long nnz, int rows) {
   int L = 1;
   while (L < 32 && L * 4 < mean) L <<= 1;
   return L;
+}
+
+// ---- loops over the CTA's part of a problem's index spaces (Spans) ----
+template <typename G>
+__device__ __forceinline__ Rng span_n(const G& g, int n) { return Rng{g.sp.nlo, n < g.sp.nhi ? n : g.sp.nhi}; }
+template <typename G>
+__device__ __forceinline__ Rng span_m(const G& g, int m) { return Rng{g.sp.mlo, m < g.sp.mhi ? m : g.sp.mhi}; }
+
+template <typename G, typename FN>
+__device__ __forceinline__ void for_rng(G& g, Rng r, FN fn) {
+  for (int i = r.lo + g.t0(); i < r.hi; i += g.ts()) fn(i);
+}
+template <typename G, typename FN>
+__device__ __forceinline__ void for_n(G& g, int n, FN fn) { for_rng(g, span_n(g, n), fn); }
+template <typename G, typename FN>
+__device__ __forceinline__ void for_m(G& g, int m, FN fn) { for_rng(g, span_m(g, m), fn); }
+
+// Rows [rg.lo, rg.hi) of M, sub-warp per row (as rows_apply_L).
+template <int L, typename T, typename G, typename XF, typename FN>
+__device__ __forceinline__ void rows_rng_L(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / L, sl = lane % L;
+  constexpr int RPW = 32 / L;
+  const int ws = g.ws();
+  for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += ws * RPW) {
+    const int r = base + sub;
+    T acc = T(0);
+    if (r < rg.hi) acc = lane_row_dot<L>(M.col, M.val, M.rowptr[r], M.rowptr[r + 1], sl, xf);
+    acc = subwarp_sum<L>(acc);
+    if (r < rg.hi && sl == 0) fn(r, acc);
+  }
+}
+template <typename T, typename G, typename XF, typename FN>
+__device__ __forceinline__ void rows_rng(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
+  switch (M.lanes) {
+    case 1:  rows_rng_L<1>(g, rg, M, xf, fn); break;
+    case 2:  rows_rng_L<2>(g, rg, M, xf, fn); break;
+    case 4:  rows_rng_L<4>(g, rg, M, xf, fn); break;
+    case 8:  rows_rng_L<8>(g, rg, M, xf, fn); break;
+    case 16: rows_rng_L<16>(g, rg, M, xf, fn); break;
+    default: rows_rng_L<32>(g, rg, M, xf, fn); break;
+  }
+}
+template <int L, typename T, typename G, typename XF1, typename XF2, typename FN>
+__device__ __forceinline__ void rows_rng2_L(G& g, Rng rg, const CSR<T>& M, XF1 xf1, XF2 xf2, FN fn) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / L, sl = lane % L;
+  constexpr int RPW = 32 / L;
+  const int ws = g.ws();
+  for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += ws * RPW) {
+    const int r = base + sub;
+    T a1 = T(0), a2 = T(0);
+    if (r < rg.hi) lane_row_dot2<L>(M.col, M.val, M.rowptr[r], M.rowptr[r + 1], sl, xf1, xf2, a1, a2);
+    a1 = subwarp_sum<L>(a1);
+    a2 = subwarp_sum<L>(a2);
+    if (r < rg.hi && sl == 0) fn(r, a1, a2);
+  }
+}
+template <typename T, typename G, typename XF1, typename XF2, typename FN>
+__device__ __forceinline__ void rows_rng2(G& g, Rng rg, const CSR<T>& M, XF1 a, XF2 b, FN fn) {
+  switch (M.lanes) {
+    case 1:  rows_rng2_L<1>(g, rg, M, a, b, fn); break;
+    case 2:  rows_rng2_L<2>(g, rg, M, a, b, fn); break;
+    case 4:  rows_rng2_L<4>(g, rg, M, a, b, fn); break;
+    case 8:  rows_rng2_L<8>(g, rg, M, a, b, fn); break;
+    case 16: rows_rng2_L<16>(g, rg, M, a, b, fn); break;
+    default: rows_rng2_L<32>(g, rg, M, a, b, fn); break;
+  }
 }
 
 // Element-wise loop over [b, e) across the group.

@@ -116,9 +116,10 @@ __device__ __forceinline__ void kkt_rows_L(G& g, const CSR<T>& P, const CSR<T>& 
   const int lane = threadIdx.x & 31;
   const int sub = lane / L, sl = lane % L;
   constexpr int RPW = 32 / L;
-  const int nw = g.nwarps(), w = g.warp();
-  const int n = P.rows;
-  for (int base = w * RPW; base < n; base += nw * RPW) {
+  const Rng rg = span_n(g, P.rows);
+  const int n = rg.hi;
+  const int ws = g.ws();
+  for (int base = rg.lo + g.w0() * RPW; base < n; base += ws * RPW) {
     const int i = base + sub;
     T a1 = T(0), a2 = T(0);
     if (i < n) {
@@ -249,7 +250,7 @@ struct Solver {
   __device__ void set_rho_vec(G& g) {
     const double infval = s.infty * kMinScaling;
     const double rho = sc->rho;
-    for_each(g, pr.m, [&](int j) {
+    for_m(g, pr.m, [&](int j) {
       const double l = pr.l[j], u = pr.u[j];
       int t;
       if (l < -infval && u > infval) t = -1;
@@ -257,17 +258,22 @@ struct Solver {
       else t = 0;
       pr.ctype[j] = t;
       const double rv = t < 0 ? kRhoMin : (t == 0 ? rho : kRhoEqOverIneq * rho);
-      pr.rho_vec[j] = (T)rv;
+      g.put(pr.rho_vec, j, (T)rv);
       pr.rho_inv_vec[j] = T(1) / (T)rv;
     });
   }
   template <typename G>
   __device__ void refresh_rho_vec(G& g) {
+    // local copies: hot loops keep the pointers in registers instead of
+    // re-reading them through `this` after every store
+    const DevProblem<T> pr = this->pr;
+    const DevSettings s = this->s;
+    SolverScalars* const sc = this->sc;
     const double rho = sc->rho;
-    for_each(g, pr.m, [&](int j) {
+    for_m(g, pr.m, [&](int j) {
       const int t = pr.ctype[j];
       const double rv = t < 0 ? kRhoMin : (t == 0 ? rho : kRhoEqOverIneq * rho);
-      pr.rho_vec[j] = (T)rv;
+      g.put(pr.rho_vec, j, (T)rv);
       pr.rho_inv_vec[j] = T(1) / (T)rv;
     });
   }
@@ -275,10 +281,15 @@ struct Solver {
   // Jacobi preconditioner M = sigma + diag(P) + diag(A' R A) (cuda_pcg.cu:211-266)
   template <typename G>
   __device__ void update_precond(G& g) {
+    // local copies: hot loops keep the pointers in registers instead of
+    // re-reading them through `this` after every store
+    const DevProblem<T> pr = this->pr;
+    const DevSettings s = this->s;
+    SolverScalars* const sc = this->sc;
     const T sig = (T)s.sigma;
     const bool vec = s.rho_is_vec;
     const T rho = (T)sc->rho;
-    for_each(g, pr.n, [&](int i) {
+    for_n(g, pr.n, [&](int i) {
       if (s.cg_precond == 0) { pr.Minv[i] = T(1); return; }
       T d = T(0);
       for (int k = pr.At.rowptr[i]; k < pr.At.rowptr[i + 1]; k++) {
@@ -292,8 +303,8 @@ struct Solver {
 
   template <typename G>
   __device__ void cold_start(G& g) {
-    for_each(g, pr.n, [&](int i) { pr.x[i] = T(0); pr.xp[i] = T(0); });
-    for_each(g, pr.m, [&](int j) { pr.z[j] = T(0); pr.y[j] = T(0); });
+    for_n(g, pr.n, [&](int i) { pr.x[i] = T(0); g.put(pr.xp, i, T(0)); });
+    for_m(g, pr.m, [&](int j) { pr.z[j] = T(0); pr.y[j] = T(0); });
   }
 
   // Values, scaling, rho vector and preconditioner.  keep = true is the matrix
@@ -335,6 +346,11 @@ struct Solver {
   // ---------------------------------------------------------------------
   template <typename G>
   __device__ bool admm_iteration(G& g, int iter) {
+    // local copies: hot loops keep the pointers in registers instead of
+    // re-reading them through `this` after every store
+    const DevProblem<T> pr = this->pr;
+    const DevSettings s = this->s;
+    SolverScalars* const sc = this->sc;
     const int n = pr.n, m = pr.m;
     const bool vec = s.rho_is_vec;
     const T sig = (T)s.sigma;
@@ -345,7 +361,7 @@ struct Solver {
     // Phase R: rhs = (sigma x - q) + A'(rho .* (z - rho^-1 y)) and t = rho .* (A xp)
     Acc<T> sm0[1];
     T mx0[3] = {T(0), T(-INFINITY), T(-INFINITY)};
-    rows_apply(g, pr.At,
+    rows_rng(g, span_n(g, n), pr.At,
       [&](int j) {
         const T rj = vec ? pr.rho_vec[j] : rho_s;
         const T ij = vec ? pr.rho_inv_vec[j] : rinv_s;
@@ -358,8 +374,8 @@ struct Solver {
         mx0[0] = tmax(mx0[0], (T)fabs(rr));
       });
     if (m > 0) {
-      rows_apply(g, pr.A, [&](int c) { return xp[c]; },
-        [&](int j, T v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
+      rows_rng(g, span_m(g, m), pr.A, [&](int c) { return xp[c]; },
+        [&](int j, T v) { g.put(pr.t, j, (vec ? pr.rho_vec[j] : rho_s) * v); });
     }
     // time / cancellation ride on this reduction so every CTA sees the same values
     if (g.tid() == 0) {
@@ -404,14 +420,14 @@ struct Solver {
 
     // Phase U: x~ = xp, z~ = A xp, then the x / z / y updates (auxil.c:172-229)
     const T al = (T)s.alpha, oma = (T)(1.0 - s.alpha);
-    for_each(g, n, [&](int i) {
+    for_n(g, n, [&](int i) {
       const T xo = x[i];
       const T xn = al * xp[i] + oma * xo;
       x[i] = xn;
       pr.dx[i] = xn - xo;
     });
     if (m > 0) {
-      rows_apply(g, pr.A, [&](int c) { return xp[c]; }, [&](int j, T zt) {
+      rows_rng(g, span_m(g, m), pr.A, [&](int c) { return xp[c]; }, [&](int j, T zt) {
         const T ri = vec ? pr.rho_inv_vec[j] : rinv_s;
         const T rr = vec ? pr.rho_vec[j] : rho_s;
         const T zo = z[j];
@@ -437,9 +453,21 @@ struct Solver {
   // ---------------------------------------------------------------------
   template <typename G>
   __device__ int pcg_core(G& g, double eps, T sig, T rho_s) {
+    // local copies: hot loops keep the pointers in registers instead of
+    // re-reading them through `this` after every store
+    const DevProblem<T> pr = this->pr;
+    const DevSettings s = this->s;
+    SolverScalars* const sc = this->sc;
     const int n = pr.n, m = pr.m;
     const bool vec = s.rho_is_vec && pr.rho_vec;
+    const int cg_max = s.cg_max_iter;
     T* __restrict__ xp = pr.xp;
+    // Scalar recurrences (rTy, alpha, beta, the stopping test) run in FP64 on
+    // one thread inside each reduction; the other threads read the results
+    // from shared memory: GB300's FP64 rate makes per-thread FP64 scalar
+    // math cost more than a whole vector phase.
+    GroupShared* gs = g.sh;
+    T* bT = bcast_slots<T>(gs);   // [0] alpha  [1] beta
     // Phase I: r = K xp - rhs, yv = M^-1 r, p = -yv, rTy, ||r||
     T* pA = sc->p_parity ? pr.p1 : pr.p0;
     Acc<T> sm1[1];
@@ -449,24 +477,27 @@ struct Solver {
         const T kx = sig * xp[i] + pv + av;
         const T r = kx - pr.rhs[i];
         const T yv = pr.Minv[i] * r;
-        pr.r[i] = r; pr.yv[i] = yv; pA[i] = -yv;
+        pr.r[i] = r; pr.yv[i] = yv; g.put(pA, i, -yv);
         sm1[0].add_prod(yv, r);
         mx1[0] = tmax(mx1[0], (T)fabs(r));
       });
     double rs1[1], rm1[1];
-    g.reduce(sm1, mx1, rs1, rm1);
+    // bd[0] = rTy, bi[0] = continue, bi[1] = iterations
+    g.reduce(sm1, mx1, rs1, rm1, [&](const double* rsum, const double* rmax) {
+      gs->bd[0] = rsum[0];
+      gs->bi[1] = 0;
+      gs->bi[0] = (rmax[0] > eps && 0 < cg_max) ? 1 : 0;
+    });
     if (!g.ok()) return -1;
-    double rTy = rs1[0], rnorm = rm1[0];
 
     // PCG loop (cuda_pcg.cu:155-200).  Four phases per iteration; each ends
     // at a group barrier (the two reductions carry theirs).
     T* p = pA;
-    int it = 0;
-    while (rnorm > eps && it < s.cg_max_iter) {
+    while (gs->bi[0]) {
       // Phase A: t = rho .* (A p)
       if (m > 0) {
-        rows_apply(g, pr.A, [&](int c) { return p[c]; },
-                   [&](int j, T v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
+        rows_rng(g, span_m(g, m), pr.A, [&](int c) { return p[c]; },
+                 [&](int j, T v) { g.put(pr.t, j, (vec ? pr.rho_vec[j] : rho_s) * v); });
         if (!g.sync()) return -1;
       }
       // Phase B: Kp = sigma p + P p + A' t ; pKp
@@ -480,15 +511,16 @@ struct Solver {
           sm2[0].add_prod(pi, kp);
         });
       double rs2[1], rm2[1];
-      g.reduce(sm2, mx2, rs2, rm2);
+      g.reduce(sm2, mx2, rs2, rm2, [&](const double* rsum, const double*) {
+        bT[0] = (T)(gs->bd[0] / rsum[0]);
+      });
       if (!g.ok()) return -1;
-      const double alpha = rTy / rs2[0];
-      const T at = (T)alpha;
+      const T at = bT[0];
       // Phase C: x += alpha p ; r += alpha Kp ; yv = M^-1 r ; rTy ; ||r||
       Acc<T> sm3[1];
       T mx3[1] = {T(0)};
-      for_each(g, n, [&](int i) {
-        xp[i] += at * p[i];
+      for_n(g, n, [&](int i) {
+        g.put(xp, i, xp[i] + at * p[i]);
         const T r = pr.r[i] + at * pr.Kp[i];
         pr.r[i] = r;
         const T yv = pr.Minv[i] * r;
@@ -497,28 +529,31 @@ struct Solver {
         mx3[0] = tmax(mx3[0], (T)fabs(r));
       });
       double rs3[1], rm3[1];
-      g.reduce(sm3, mx3, rs3, rm3);
+      g.reduce(sm3, mx3, rs3, rm3, [&](const double* rsum, const double* rmax) {
+        const double rTy_new = rsum[0];
+        bT[1] = (T)(rTy_new / gs->bd[0]);
+        gs->bd[0] = rTy_new;
+        const int it = gs->bi[1] + 1;
+        gs->bi[1] = it;
+        gs->bi[0] = (rmax[0] > eps && it < cg_max) ? 1 : 0;
+      });
       if (!g.ok()) return -1;
-      const double rTy_new = rs3[0];
-      const double beta = rTy_new / rTy;
-      rTy = rTy_new;
-      rnorm = rm3[0];
-      it++;
       // Phase D: p = beta p - yv (skipped when the loop is about to end)
-      if (rnorm > eps && it < s.cg_max_iter) {
-        const T bt = (T)beta;
-        for_each(g, n, [&](int i) { p[i] = bt * p[i] - pr.yv[i]; });
+      if (gs->bi[0]) {
+        const T bt = bT[1];
+        for_n(g, n, [&](int i) { g.put(p, i, bt * p[i] - pr.yv[i]); });
         if (!g.sync()) return -1;
       }
     }
+    const int it = gs->bi[1];
     if (threadIdx.x == 0) {
       sc->pcg_iters_total += it;
       if (it == 0) sc->zero_pcg_iters++; else sc->zero_pcg_iters = 0;
     }
     __syncthreads();
     return it;
-
   }
+
 
   // Reduced-KKT solve behind the linear-system interface (LinSysSolver.solve,
   // cuda_pcg_interface.cu:229-273): b = [b1; b2] in, [x~; A x~] out
@@ -526,6 +561,11 @@ struct Solver {
   // cuda_pcg_interface.cu:32-64 with the caller's scaled residuals.
   template <typename G>
   __device__ bool linsys_solve(G& g, T* b, int admm_iter, bool polishing, double spr, double sdr) {
+    // local copies: hot loops keep the pointers in registers instead of
+    // re-reading them through `this` after every store
+    const DevProblem<T> pr = this->pr;
+    const DevSettings s = this->s;
+    SolverScalars* const sc = this->sc;
     const int n = pr.n, m = pr.m;
     const bool vec = s.rho_is_vec && pr.rho_vec;
     const T sig = (T)s.sigma;
@@ -535,15 +575,15 @@ struct Solver {
     T* b2 = b + n;
     Acc<T> sm0[1];
     T mx0[1] = {T(0)};
-    rows_apply(g, pr.At, [&](int j) { return (vec ? pr.rho_vec[j] : rho_s) * b2[j]; },
+    rows_rng(g, span_n(g, n), pr.At, [&](int j) { return (vec ? pr.rho_vec[j] : rho_s) * b2[j]; },
                [&](int i, T v) {
                  const T rr = b1[i] + v;
                  pr.rhs[i] = rr;
                  mx0[0] = tmax(mx0[0], (T)fabs(rr));
                });
     if (m > 0)
-      rows_apply(g, pr.A, [&](int c) { return xp[c]; },
-                 [&](int j, T v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
+      rows_rng(g, span_m(g, m), pr.A, [&](int c) { return xp[c]; },
+               [&](int j, T v) { g.put(pr.t, j, (vec ? pr.rho_vec[j] : rho_s) * v); });
     double rs0[1], rm0[1];
     g.reduce(sm0, mx0, rs0, rm0);
     if (!g.ok()) return false;
@@ -567,10 +607,10 @@ struct Solver {
     const double eps = sc->pcg_eps;
     if (pcg_core(g, eps, sig, rho_s) < 0) return false;
     // outputs: b1 <- x ; b2 <- A x  (or (A x - b2) / delta when polishing)
-    for_each(g, n, [&](int i) { b[i] = xp[i]; });
+    for_n(g, n, [&](int i) { b[i] = xp[i]; });
     if (m > 0) {
       const T rp = (T)sc->rho;
-      rows_apply(g, pr.A, [&](int c) { return xp[c]; },
+      rows_rng(g, span_m(g, m), pr.A, [&](int c) { return xp[c]; },
                  [&](int j, T v) { b2[j] = polishing ? (v - b2[j]) * rp : v; });
     }
     return g.sync();
@@ -581,6 +621,11 @@ struct Solver {
   // ---------------------------------------------------------------------
   template <typename G>
   __device__ bool update_info(G& g, int iter) {
+    // local copies: hot loops keep the pointers in registers instead of
+    // re-reading them through `this` after every store
+    const DevProblem<T> pr = this->pr;
+    const DevSettings s = this->s;
+    SolverScalars* const sc = this->sc;
     const int n = pr.n, m = pr.m;
     const double infval = s.infty * kMinScaling;
     const bool uns = unscaled_term();
@@ -595,7 +640,7 @@ struct Solver {
 #pragma unroll
     for (int k = 0; k < 9; k++) mx[k] = (k == 8) ? T(-INFINITY) : T(0);
     if (m > 0) {
-      rows_apply2(g, pr.A, [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; },
+      rows_rng2(g, span_m(g, m), pr.A, [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; },
         [&](int j, T ax, T adx) {
           const T l = pr.l[j], u = pr.u[j];
           const T ei = pr.Einv[j];
@@ -652,11 +697,12 @@ struct Solver {
         const int lane = threadIdx.x & 31;
         const int sub = lane / LL, sl = lane % LL;
         constexpr int RPW = 32 / LL;
-        const int nw = g.nwarps(), w = g.warp();
-        for (int base = w * RPW; base < n; base += nw * RPW) {
+        const Rng rg = span_n(g, n);
+        const int ws = g.ws();
+        for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += ws * RPW) {
           const int i = base + sub;
           T px = T(0), pdx = T(0), aty = T(0), atdy = T(0);
-          if (i < n) {
+          if (i < rg.hi) {
             lane_row_dot2<LL>(pr.P.col, pr.P.val, pr.P.rowptr[i], pr.P.rowptr[i + 1], sl,
                               [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; }, px, pdx);
             lane_row_dot2<LL>(pr.At.col, pr.At.val, pr.At.rowptr[i], pr.At.rowptr[i + 1], sl,
@@ -664,7 +710,7 @@ struct Solver {
           }
           px = subwarp_sum<LL>(px); pdx = subwarp_sum<LL>(pdx);
           aty = subwarp_sum<LL>(aty); atdy = subwarp_sum<LL>(atdy);
-          if (i < n && sl == 0) {
+          if (i < rg.hi && sl == 0) {
             const T q = pr.q[i];
             const T di = pr.Dinv[i];
             const T dr = (m > 0) ? (q + px) + aty : q + px;
@@ -795,20 +841,30 @@ struct Solver {
   // ---------------------------------------------------------------------
   // The solve loop (osqp_api.c:636-1038)
   // ---------------------------------------------------------------------
+  //
+  // Iterations it_lo..it_hi of the loop.  A solve that reaches it_hi before
+  // max_iter without terminating is suspended: status stays ST_UNSOLVED,
+  // sc->iter = it_hi, and every iterate stays in place, so a later call with
+  // it_lo = it_hi + 1 (by any group form) continues exactly where it stopped.
   template <typename G>
-  __device__ bool solve(G& g) {
+  __device__ bool solve(G& g, int it_lo = 1, int it_hi = 0x7fffffff) {
     __shared__ int s_flags[4];
     if (threadIdx.x == 0) {
-      sc->t_start = global_ns();
       s_flags[0] = 0;
-      sc->status = ST_UNSOLVED;
-      sc->pcg_iters_total = 0;
+      if (it_lo <= 1) {
+        sc->t_start = global_ns();
+        sc->status = ST_UNSOLVED;
+        sc->pcg_iters_total = 0;
+      }
     }
-    if (!s.warm_starting) { cold_start(g); }
+    if (it_lo <= 1 && !s.warm_starting) { cold_start(g); }
     if (!g.sync()) return false;
+    if (it_lo < 1) it_lo = 1;
+    const int it_end = it_hi < s.max_iter ? it_hi : s.max_iter;
     int can_check = 0;
     int iter;
-    for (iter = 1; iter <= s.max_iter; iter++) {
+    bool stopped = false;
+    for (iter = it_lo; iter <= it_end; iter++) {
       if (!admm_iteration(g, iter)) return false;
       if (threadIdx.x == 0) {
         int stop = 0;
@@ -822,7 +878,7 @@ struct Solver {
         s_flags[1] = cc; s_flags[2] = ca;
       }
       __syncthreads();
-      if (s_flags[0]) break;
+      if (s_flags[0]) { stopped = true; break; }
       can_check = s_flags[1];
       int can_adapt = s_flags[2];
       if (can_check || can_adapt || iter == 1) { if (!update_info(g, iter)) return false; }
@@ -847,12 +903,18 @@ struct Solver {
         }
       }
       __syncthreads();
-      if (s_flags[3]) break;
+      if (s_flags[3]) { stopped = true; break; }
       if (sc->rho_updated) {
         if (s.rho_is_vec) { refresh_rho_vec(g); if (!g.sync()) return false; }
         update_precond(g);
         if (!g.sync()) return false;
       }
+    }
+    if (!stopped && it_end < s.max_iter) {
+      // suspended at it_hi: no post-loop, no solution store
+      if (threadIdx.x == 0) sc->iter = it_end;
+      __syncthreads();
+      return g.sync();
     }
     // post-loop (osqp_api.c:906-960); an interrupted solve skips it, as the
     // reference jumps to its exit label on SIGINT
@@ -883,15 +945,20 @@ struct Solver {
   // store_solution (auxil.c:598-674) into xo / yo / pcert / dcert
   template <typename G>
   __device__ bool store_solution(G& g) {
+    // local copies: hot loops keep the pointers in registers instead of
+    // re-reading them through `this` after every store
+    const DevProblem<T> pr = this->pr;
+    const DevSettings s = this->s;
+    SolverScalars* const sc = this->sc;
     const int st = sc->status, n = pr.n, m = pr.m;
     const bool uns = unscaled_term();
     if (has_solution(st)) {
       const T cinv = (T)sc->cinv;
-      for_each(g, n, [&](int i) {
+      for_n(g, n, [&](int i) {
         pr.xo[i] = s.scaling ? pr.D[i] * pr.x[i] : pr.x[i];
         pr.dcert[i] = tnan<T>(); pr.dx[i] = tnan<T>();
       });
-      for_each(g, m, [&](int j) {
+      for_m(g, m, [&](int j) {
         pr.yo[j] = s.scaling ? (pr.E[j] * pr.y[j]) * cinv : pr.y[j];
         pr.pcert[j] = tnan<T>(); pr.dy[j] = tnan<T>();
       });
@@ -900,23 +967,23 @@ struct Solver {
     const bool pinf = st == ST_PRIMAL_INFEASIBLE || st == ST_PRIMAL_INFEASIBLE_INACCURATE;
     const bool dinf = st == ST_DUAL_INFEASIBLE || st == ST_DUAL_INFEASIBLE_INACCURATE;
     // certificates in the user's scaling (auxil.c:914-935)
-    if (pinf && uns) for_each(g, m, [&](int j) { pr.dy[j] *= pr.E[j]; });
-    if (dinf && uns) for_each(g, n, [&](int i) { pr.dx[i] *= pr.D[i]; });
+    if (pinf && uns) for_m(g, m, [&](int j) { pr.dy[j] *= pr.E[j]; });
+    if (dinf && uns) for_n(g, n, [&](int i) { pr.dx[i] *= pr.D[i]; });
     if (!g.sync()) return false;
     Acc<T> sm[1];
     T mx[2] = {T(0), T(0)};
-    for_each(g, m, [&](int j) { mx[0] = tmax(mx[0], (T)fabs(pr.dy[j])); });
-    for_each(g, n, [&](int i) { mx[1] = tmax(mx[1], (T)fabs(pr.dx[i])); });
+    for_m(g, m, [&](int j) { mx[0] = tmax(mx[0], (T)fabs(pr.dy[j])); });
+    for_n(g, n, [&](int i) { mx[1] = tmax(mx[1], (T)fabs(pr.dx[i])); });
     double smr[1], mxr[2];
     g.reduce(sm, mx, smr, mxr);
     if (!g.ok()) return false;
     const T iny = (T)(1.0 / mxr[0]), inx = (T)(1.0 / mxr[1]);
-    for_each(g, n, [&](int i) {
+    for_n(g, n, [&](int i) {
       pr.xo[i] = tnan<T>();
       pr.dcert[i] = dinf ? pr.dx[i] * inx : tnan<T>();
-      pr.x[i] = T(0); pr.xp[i] = T(0);
+      pr.x[i] = T(0); g.put(pr.xp, i, T(0));
     });
-    for_each(g, m, [&](int j) {
+    for_m(g, m, [&](int j) {
       pr.yo[j] = tnan<T>();
       pr.pcert[j] = pinf ? pr.dy[j] * iny : tnan<T>();
       pr.z[j] = T(0); pr.y[j] = T(0);
