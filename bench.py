@@ -273,7 +273,7 @@ def gpu_arm(args, probs, ls, us):
     # ---- plain one-QP-at-a-time GPU form on a sample (the reference's usage pattern) ----
     plain = None
     if rank == 0 and args.plain_sample > 0:
-        os.environ.setdefault("OSQP_GB300_MODE", "grid")
+        # the library picks the execution form for a single QP (CTA, cluster or grid)
         tt = 0.0
         ns = min(args.plain_sample, count)
         moff = np.concatenate([[0], np.cumsum([p[2].shape[0] for p in probs])])

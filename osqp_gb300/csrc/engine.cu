@@ -24,6 +24,7 @@
 #include "gb_solver.cuh"
 #include "gb_structure.cuh"
 #include "gb_launch.cuh"
+#include "gb_engine.h"
 
 using T = OSQPFloat;
 using namespace gb;
@@ -1039,7 +1040,16 @@ extern "C" OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter
   return 0;
 }
 
-// Device pointers of the workspace (used by the polish stage and by tests).
-DevProblem<T>* gb_problem(OSQPSolver* solver) { return &solver->work->pr; }
-cudaStream_t gb_stream(OSQPSolver* solver) { return solver->work->stream; }
+// The workspace as the polish stage sees it.
+GbEngineView gb_engine_view(OSQPSolver* solver) {
+  OSQPWorkspace* w = solver->work;
+  GbEngineView v;
+  v.pr = w->pr; v.ds = w->ds;
+  v.n = w->n; v.m = w->m; v.nnzA = w->nnzA; v.nnzPf = w->nnzPf;
+  v.use_grid = w->use_grid; v.grid_blocks = w->grid_blocks;
+  grid_sync_args(w, v.gs);
+  v.stream = w->stream;
+  v.h_st = w->h_st;
+  return v;
+}
 
