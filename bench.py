@@ -31,6 +31,11 @@ import argparse
 import json
 import multiprocessing as mp
 import os
+
+# Independent launches on separate streams (the served form) must not share
+# hardware queues behind long-running kernels: the default of 8 connections
+# serialised concurrent launches.  Set before the CUDA context exists.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import subprocess
 import sys
 import time
@@ -277,7 +282,7 @@ def gpu_arm(args, probs, ls, us):
         tt = 0.0
         ns = min(args.plain_sample, count)
         moff = np.concatenate([[0], np.cumsum([p[2].shape[0] for p in probs])])
-        for k in range(ns):
+        for k in range(0, count, max(1, count // ns))[:ns]:   # every (count/ns)-th QP
             s1 = OSQP(lib)
             s1.setup(*probs[k], **settings)
             s1.update(l=ls[W][moff[k]:moff[k + 1]], u=us[W][moff[k]:moff[k + 1]])
@@ -303,6 +308,91 @@ def gpu_arm(args, probs, ls, us):
     return out
 
 
+# ---------------------------------------------------------------------------
+# Served form: Poisson request stream over resident pools (continuous batching)
+# ---------------------------------------------------------------------------
+def serve_leg(args):
+    """50% MPC and 50% factor-model portfolio requests from `streams` recurring
+    problems each, Poisson arrivals at `rate` req/s for `seconds`.  Each
+    stream's data drift between its requests: an MPC stream's measured state
+    x0 follows a random walk (step N(0, 0.05) per request, clipped to [-1, 1])
+    -> new bounds; a portfolio stream's mean returns drift (x (1 + 0.02 N(0,1)))
+    -> new q.  Every stream keeps its structure, scaling and warm-start iterates
+    resident.  Latency = submission to results on the host."""
+    import threading
+    from osqp_gb300 import load
+    from osqp_gb300.api import Batch, Server
+    lib = load("f32")
+    S = args.serve_streams
+    mpc = pb.mpc_batch(S, seed=11)
+    port = [pb.portfolio(seed=20000 + i) for i in range(S)]
+    st = dict(SETTINGS, warm_starting=1)
+    pools = []
+    for probs in (mpc, port):
+        b = Batch(lib)
+        assert b.setup(probs, **st) == 0, "pool set-up refused"
+        pools.append(b)
+    srv = Server(lib, concurrency=args.serve_concurrency)
+    pid = [srv.add_pool(b) for b in pools]
+    nxs = [_nx_of(p[2]) for p in mpc]
+    rg = np.random.default_rng([11, 3])
+    n_req = int(args.serve_rate * args.serve_seconds)
+    t_arr = np.cumsum(rg.exponential(1.0 / args.serve_rate, n_req))
+    kind = rg.integers(0, 2, n_req)
+    which = rg.integers(0, S, n_req)
+    payload = []
+    x0 = [-mpc[i][3][:nxs[i]].copy() for i in range(S)]     # each MPC stream's current state
+    for k, i in zip(kind, which):
+        if k == 0:
+            P, q, A, l, u = mpc[i]
+            x0[i] = np.clip(x0[i] + 0.05 * rg.standard_normal(nxs[i]), -1.0, 1.0)
+            l2, u2 = pb.mpc_x0_bounds(l, u, x0[i])
+            payload.append((pid[0], int(i), None, l2.astype(np.float32), u2.astype(np.float32), P.shape[0]))
+        else:
+            P, q, A, l, u = port[i]
+            q2 = (q * (1.0 + 0.02 * rg.standard_normal(q.size))).astype(np.float32)
+            payload.append((pid[1], int(i), q2, None, None, P.shape[0]))
+    # warm-up: one request per stream (cold start of every stream), untimed
+    for j, probs in enumerate((mpc, port)):
+        ts = [srv.submit(pid[j], i) for i in range(S)]
+        for i, t in enumerate(ts):
+            srv.wait(t, probs[i][0].shape[0])
+    tickets = [None] * n_req
+    t0 = time.perf_counter()
+
+    def submitter():
+        for r in range(n_req):
+            dt = t0 + t_arr[r] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            pl, i, q2, l2, u2, _ = payload[r]
+            tickets[r] = srv.submit(pl, i, q2, l2, u2)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat, stat, its = np.zeros(n_req), np.zeros(n_req, np.int32), np.zeros(n_req, np.int32)
+    for r in range(n_req):
+        while tickets[r] is None:
+            time.sleep(1e-5)
+        _, stat[r], its[r], _, lat[r] = srv.wait(tickets[r], payload[r][5])
+    elapsed = time.perf_counter() - t0
+    th.join()
+    srv.close()
+    for b in pools:
+        b.cleanup()
+    mk = kind == 0
+    return {"rate_rps": args.serve_rate, "seconds": args.serve_seconds, "requests": n_req,
+            "streams": {"mpc": S, "portfolio": S}, "concurrency": args.serve_concurrency,
+            "solves_per_s": n_req / elapsed, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "p50_ms_mpc": float(np.percentile(lat[mk], 50)),
+            "p99_ms_mpc": float(np.percentile(lat[mk], 99)),
+            "p50_ms_portfolio": float(np.percentile(lat[~mk], 50)),
+            "p99_ms_portfolio": float(np.percentile(lat[~mk], 99)),
+            "admm_iters_mean": float(its.mean()), "admm_iters_mean_mpc": float(its[mk].mean()),
+            "admm_iters_mean_portfolio": float(its[~mk].mean()),
+            "status_counts": {int(k): int(v) for k, v in zip(*np.unique(stat, return_counts=True))}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -310,8 +400,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--count", type=int, default=4096)
-    ap.add_argument("--plain-sample", type=int, default=8)
+    ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--serve-rate", type=float, default=100.0, help="served form: Poisson arrivals (req/s); 0 = skip")
+    ap.add_argument("--serve-seconds", type=float, default=4.0)
+    ap.add_argument("--serve-streams", type=int, default=128, help="recurring problems per class")
+    ap.add_argument("--serve-concurrency", type=int, default=16, help="launches in flight")
     ap.add_argument("--max-iter", type=int, default=SETTINGS["max_iter"],
                     help="ADMM iteration cap (smaller values give short profiling cases)")
     args = ap.parse_args()
@@ -345,6 +439,7 @@ def main():
     g = gpu_arm(args, probs, ls, us)
     if rank != 0:
         return
+    served = serve_leg(args) if args.serve_rate > 0 else None
     peak, peak_kind = measured_peak()
     sizes_m = [p[2].shape[0] for p in probs]
     cpu = cpu_arm(probs, [ls[W]], [us[W]], sizes_m, budget_s=args.cpu_budget, steps=1) if args.cpu_budget > 0 else None
@@ -374,6 +469,7 @@ def main():
         batched_over_plain=(g["value"] / g["plain"]) if g["plain"] else None,
         admm_iters_per_qp=g["admm_per_qp"], pcg_iters_per_qp=g["pcg_per_qp"],
         status_counts=g["status_counts"], objective_vs_fp64_oracle=obj_err,
+        served=served,
     )
     print(json.dumps(line))
 

@@ -22,11 +22,12 @@ OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter, long long
                                double* kernel_ms, OSQPInt* grid_form);
 
 /* ---- Batched solver --------------------------------------------------------
- * Many independent QPs of uneven size solved in one persistent launch: one
- * CTA runs the complete OSQP algorithm (scaling, ADMM, reduced-KKT PCG,
- * termination, adaptive rho) for one QP at a time, pulling QPs from a device
- * work queue ordered by decreasing size.  Results are identical to solving
- * each QP alone with the same settings (same launch shape per QP).
+ * Many independent QPs of uneven size solved in one persistent launch: a CTA
+ * (or a thread-block cluster) runs the complete OSQP algorithm (scaling, ADMM,
+ * reduced-KKT PCG, termination, adaptive rho) for one QP at a time, pulling
+ * QPs from a device work queue ordered by decreasing size; QPs still running
+ * after a fixed ADMM iteration continue on a cluster of CTAs.  A QP's result
+ * does not depend on the other QPs of the batch.
  *
  * Packed input: for QP k with sizes n[k], m[k]
  *   P: upper-triangular CSC, column pointers Pp (n[k]+1 entries, starting at 0)
@@ -71,6 +72,42 @@ OSQPInt osqp_gb300_batch_step_ms(OSQPBatch* batch, double* step_ms);
 OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* batch, long long* pcg_iter);
 
 OSQPInt osqp_gb300_batch_cleanup(OSQPBatch* batch);
+
+/* ---- Request serving (continuous batching) ---------------------------------
+ * A server owns a worker thread and `concurrency` CUDA streams.  QPs are made
+ * resident as pools (batches set up with osqp_gb300_batch_setup; set-up is
+ * refused with OSQP_MEM_ALLOC_ERROR when free device memory does not hold the
+ * pool): structures, scaling, preconditioner and warm-start iterates stay in
+ * device memory between requests.  A request names a pool, a QP of it and
+ * optional new q / l / u (host memory, QP-sized; NULL keeps the current
+ * vector).  Requests that arrive while others are on the device are launched
+ * as soon as a stream is free: every free stream takes the waiting requests of
+ * one pool (at most one per QP at a time, at most the pool's resident CTA
+ * slots / concurrency) as one launch, so work from different arrivals
+ * overlaps on the device.  A request's result is the same whatever
+ * else is in flight.  A pool served by a server must not be used through the
+ * batch calls meanwhile. */
+typedef struct OSQPServer_ OSQPServer;
+
+OSQPInt osqp_gb300_server_create(OSQPServer** server, OSQPInt concurrency);
+
+/* Register a pool; returns its id in *pool_id. */
+OSQPInt osqp_gb300_server_add_pool(OSQPServer* server, OSQPBatch* pool, OSQPInt* pool_id);
+
+/* Queue a solve of QP `qp` of pool `pool_id`; returns a ticket.  The vectors
+ * are copied before the call returns. */
+OSQPInt osqp_gb300_server_submit(OSQPServer* server, OSQPInt pool_id, OSQPInt qp, const OSQPFloat* q,
+                                 const OSQPFloat* l, const OSQPFloat* u, long long* ticket);
+
+/* Wait for a ticket; copies x (QP-sized, host memory, may be NULL), status,
+ * iterations, objective and the request's latency in ms (submission to
+ * results on the host).  Each ticket can be waited for once. */
+OSQPInt osqp_gb300_server_wait(OSQPServer* server, long long ticket, OSQPFloat* x, OSQPInt* status,
+                               OSQPInt* iter, OSQPFloat* obj_val, double* latency_ms);
+
+/* Stop the worker after the queued requests complete and free the server
+ * (the pools stay owned by the caller). */
+OSQPInt osqp_gb300_server_destroy(OSQPServer* server);
 
 #ifdef __cplusplus
 }

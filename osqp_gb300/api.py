@@ -433,6 +433,76 @@ class Batch:
             pass
 
 
+class Server:
+    """Request serving with continuous batching (osqp_gb300_server_* in osqp_gb300_ext.h).
+
+    Pools are Batch objects whose QPs stay resident on the device; submit()
+    queues a solve of one QP of a pool with optional new q / l / u and returns
+    a ticket; wait() returns (x, status, iter, obj, latency_ms)."""
+
+    def __init__(self, library: Library, concurrency: int = 4):
+        self.L = library
+        L, F, I = library.lib, library.F, library.I
+        PF = C.POINTER(F)
+        L.osqp_gb300_server_create.argtypes = [C.POINTER(C.c_void_p), I]
+        L.osqp_gb300_server_create.restype = I
+        L.osqp_gb300_server_add_pool.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(I)]
+        L.osqp_gb300_server_add_pool.restype = I
+        L.osqp_gb300_server_submit.argtypes = [C.c_void_p, I, I, PF, PF, PF, C.POINTER(C.c_longlong)]
+        L.osqp_gb300_server_submit.restype = I
+        L.osqp_gb300_server_wait.argtypes = [C.c_void_p, C.c_longlong, PF, C.POINTER(I), C.POINTER(I), PF,
+                                             C.POINTER(C.c_double)]
+        L.osqp_gb300_server_wait.restype = I
+        L.osqp_gb300_server_destroy.argtypes = [C.c_void_p]
+        L.osqp_gb300_server_destroy.restype = I
+        self._h = C.c_void_p()
+        rc = L.osqp_gb300_server_create(C.byref(self._h), concurrency)
+        if rc:
+            raise RuntimeError(f"osqp_gb300_server_create failed: {rc}")
+        self.pools = []
+
+    def add_pool(self, batch: "Batch") -> int:
+        pid = self.L.I()
+        rc = self.L.lib.osqp_gb300_server_add_pool(self._h, batch._h, C.byref(pid))
+        if rc:
+            raise RuntimeError(f"osqp_gb300_server_add_pool failed: {rc}")
+        self.pools.append(batch)
+        return int(pid.value)
+
+    def submit(self, pool: int, qp: int, q=None, l=None, u=None) -> int:
+        F = self.L.F
+        fdt = self.L.np_float
+        conv = lambda v: None if v is None else np.ascontiguousarray(v, dtype=fdt)
+        qa, la, ua = conv(q), conv(l), conv(u)
+        t = C.c_longlong()
+        rc = self.L.lib.osqp_gb300_server_submit(self._h, pool, qp, _ptr(qa, F), _ptr(la, F), _ptr(ua, F),
+                                                 C.byref(t))
+        if rc:
+            raise ValueError(f"osqp_gb300_server_submit failed: {rc}")
+        return int(t.value)
+
+    def wait(self, ticket: int, n: int):
+        L, F, I = self.L, self.L.F, self.L.I
+        x = np.zeros(n, L.np_float)
+        st, it, ob, lat = I(), I(), F(), C.c_double()
+        rc = L.lib.osqp_gb300_server_wait(self._h, ticket, _ptr(x, F), C.byref(st), C.byref(it), C.byref(ob),
+                                          C.byref(lat))
+        if rc:
+            raise RuntimeError(f"osqp_gb300_server_wait failed: {rc}")
+        return x, int(st.value), int(it.value), float(ob.value), float(lat.value)
+
+    def close(self):
+        if self._h:
+            self.L.lib.osqp_gb300_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def objective(P, q, x) -> float:
     """0.5 x'Px + q'x with P given full or upper-triangular (symmetrised here)."""
     P = sp.csc_matrix(P)

@@ -30,7 +30,13 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
 #include <type_traits>
+#include <unordered_map>
 #include <numeric>
 #include <vector>
 
@@ -468,6 +474,19 @@ __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out,
   }
 }
 
+// Results of the QPs listed in order[0..count) (serving launches).
+__global__ void k_serve_info(const SolverScalars* st, const int* order, int count, BatchInfo* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const SolverScalars& c = st[order[i]];
+    out[i].status = c.status;
+    out[i].iter = c.iter;
+    out[i].pcg = c.pcg_iters_total;
+    out[i].obj = c.obj_val;
+    out[i].prim = c.prim_res;
+    out[i].dual = c.dual_res;
+  }
+}
+
 }  // namespace gbb
 
 using namespace gbb;
@@ -570,37 +589,60 @@ static DevSettings batch_dev_settings(const OSQPSettings* st) {
   return d;
 }
 
-static int run_batch_kernel(OSQPBatch* b, int mode) {
-  BT_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream));
-  BatchLaunch L{b->count, nullptr, b->d_queue, b->d_order, mode, 1, 0x7fffffff, 0};
-  const bool split = mode == kModeSolve && b->split > 0 && b->split < b->ds.max_iter && b->cluster < b->tail_cluster;
+// Device work list of one launch: `count` instances in `order`, plus the
+// launch's own queue counters and tail list, so launches over disjoint
+// instance sets can run concurrently on different streams.
+struct LaunchBufs {
+  const int* order;
+  int count;
+  int* queue;     // [3]: main queue, tail queue, tail count
+  int* order2;    // [count] tail list
+};
+
+// allow_split = false keeps every QP of the launch in the first form: a
+// serving launch must not wait for a whole cluster of idle SMs while other
+// launches occupy the GPU.
+static int launch_batch(OSQPBatch* b, int mode, const LaunchBufs& lb, cudaStream_t st, bool allow_split = true) {
+  int* q1 = lb.queue;
+  int* q2 = lb.queue + 1;
+  int* c2 = lb.queue + 2;
+  BT_TRY(cudaMemsetAsync(lb.queue, 0, 3 * sizeof(int), st));
+  BatchLaunch L{lb.count, nullptr, q1, lb.order, mode, 1, 0x7fffffff, 0};
+  const bool split = allow_split && mode == kModeSolve && b->split > 0 && b->split < b->ds.max_iter &&
+                     b->cluster < b->tail_cluster;
   if (split) L.it_hi = b->split;
+  const int grid = std::max(1, std::min(lb.count, b->grid));   // a small launch leaves SMs to others
   if (b->cluster >= 1) {
     L.dsm_bytes = mode == kModeSolve ? b->cdsm : 0;
-    BT_TRY(launch_clusters_dsm(b->cfn, b->grid, b->cluster, b->cthreads, (size_t)b->cdsm, b->stream, b->B, b->ds, L));
+    BT_TRY(launch_clusters_dsm(b->cfn, grid, b->cluster, b->cthreads, (size_t)b->cdsm, st, b->B, b->ds, L));
   } else {
     L.dsm_bytes = mode == kModeSolve ? b->dsm : 0;
-    b->kfn<<<b->grid, b->threads, (size_t)L.dsm_bytes, b->stream>>>(b->B, b->ds, L);
+    b->kfn<<<grid, b->threads, (size_t)L.dsm_bytes, st>>>(b->B, b->ds, L);
     BT_TRY(cudaGetLastError());
   }
   if (split) {
     // QPs still running after `split` iterations continue, from where they
     // stopped, with a cluster of CTAs each: the slowest QPs set the makespan
-    k_batch_unfinished<<<1, 1024, 0, b->stream>>>(b->B.st, b->d_order, b->count, b->d_order2, b->d_count2);
+    k_batch_unfinished<<<1, 1024, 0, st>>>(b->B.st, lb.order, lb.count, lb.order2, c2);
     BT_TRY(cudaGetLastError());
-    BT_TRY(cudaMemsetAsync(b->d_queue2, 0, sizeof(int), b->stream));
-    BatchLaunch T2{0, b->d_count2, b->d_queue2, b->d_order2, kModeSolve, b->split + 1, 0x7fffffff, 0};
+    BatchLaunch T2{0, c2, q2, lb.order2, kModeSolve, b->split + 1, 0x7fffffff, 0};
+    const int tgrid = std::max(1, std::min(lb.count, b->tail_grid));
     if (b->tail_cluster >= 1) {
       T2.dsm_bytes = b->cdsm;
-      BT_TRY(launch_clusters_dsm(b->cfn, b->tail_grid, b->tail_cluster, b->cthreads, (size_t)b->cdsm, b->stream,
+      BT_TRY(launch_clusters_dsm(b->cfn, tgrid, b->tail_cluster, b->cthreads, (size_t)b->cdsm, st,
                                  b->B, b->ds, T2));
     } else {
       T2.dsm_bytes = b->dsm;
-      b->kfn<<<b->grid, b->threads, (size_t)b->dsm, b->stream>>>(b->B, b->ds, T2);
+      b->kfn<<<grid, b->threads, (size_t)b->dsm, st>>>(b->B, b->ds, T2);
       BT_TRY(cudaGetLastError());
     }
   }
   return 0;
+}
+
+static int run_batch_kernel(OSQPBatch* b, int mode) {
+  LaunchBufs lb{b->d_order, b->count, b->d_queue2, b->d_order2};
+  return launch_batch(b, mode, lb, b->stream);
 }
 
 extern "C" OSQPInt osqp_gb300_batch_cleanup(OSQPBatch* b) {
@@ -721,6 +763,16 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   size_t o_order2 = pl.take(sizeof(int) * count);
   size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 2);
   size_t o_sq = pl.take(sizeof(T) * nsum), o_sl = pl.take(sizeof(T) * msum), o_su = pl.take(sizeof(T) * msum);
+  {
+    // admission by free device memory: refuse (rather than fail part-way)
+    // when the pool and the set-up scratch would not fit
+    size_t fr = 0, tot = 0;
+    const size_t scratch = (size_t)(2 * pto + nsum) * 24 + (size_t)ao * 16 + (64u << 20);
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && pl.off + scratch > fr) {
+      osqp_gb300_batch_cleanup(b);
+      return OSQP_MEM_ALLOC_ERROR;
+    }
+  }
   if (cudaMalloc(&b->arena, pl.off) != cudaSuccess) { osqp_gb300_batch_cleanup(b); return OSQP_MEM_ALLOC_ERROR; }
   char* a = b->arena;
   cudaStream_t s = b->stream;
@@ -736,7 +788,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   b->d_inst = (BatchInst*)(a + o_inst); B.inst = b->d_inst;
   b->d_order = (int*)(a + o_order);
   b->d_queue = (int*)(a + o_misc); b->d_flag = b->d_queue + 1;
-  b->d_queue2 = b->d_queue + 2; b->d_count2 = b->d_queue + 3; b->d_order2 = (int*)(a + o_order2);
+  b->d_queue2 = b->d_queue + 2; b->d_count2 = b->d_queue + 4; b->d_order2 = (int*)(a + o_order2);
   b->d_info = (BatchInfo*)(a + o_info); b->d_totals = (long long*)(a + o_tot);
   b->stage_q = (T*)(a + o_sq); b->stage_l = (T*)(a + o_sl); b->stage_u = (T*)(a + o_su);
 
@@ -935,5 +987,324 @@ extern "C" OSQPInt osqp_gb300_batch_stats(OSQPBatch* b, double* kernel_ms, long 
   if (kernel_ms) *kernel_ms = b->last_ms;
   if (admm_iter) *admm_iter = b->last_admm;
   if (pcg_iter) *pcg_iter = b->last_pcg;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Request serving: continuous batching over resident pools
+// ---------------------------------------------------------------------------
+namespace gbs {
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct ServeReq {
+  long long ticket = 0;
+  int pool = 0, qp = 0;
+  std::vector<T> q, l, u;
+  double t0 = 0.0, t1 = 0.0;
+  std::vector<T> x;
+  int status = 0, iter = 0;
+  double obj = 0.0;
+  bool done = false;
+};
+
+// One CUDA stream and the buffers of the launch in flight on it.
+struct Slot {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev = nullptr;
+  int cap = 0;                 // requests per launch the buffers hold
+  int* d_buf = nullptr;        // order[cap], order2[cap], queue[3]
+  BatchInfo* d_info = nullptr;
+  int* h_order = nullptr;      // pinned
+  BatchInfo* h_info = nullptr; // pinned
+  T* h_vec = nullptr;          // pinned staging: vectors in, x out
+  size_t vec_cap = 0;
+  std::vector<ServeReq*> reqs;
+  int pool = -1;
+  bool busy = false;
+};
+
+}  // namespace gbs
+
+using namespace gbs;
+
+struct OSQPServer_ {
+  int device = 0;
+  std::vector<OSQPBatch*> pools;
+  std::vector<std::vector<char>> busy;   // per pool, per QP: a request is in flight
+  std::vector<Slot> slots;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<ServeReq*> pending;
+  std::unordered_map<long long, ServeReq*> reqs;
+  long long next_ticket = 1;
+  bool stop = false;
+  int err = 0;
+  std::thread worker;
+};
+
+static int slot_reserve(Slot& sl, int cap, size_t vec) {
+  if (cap > sl.cap) {
+    if (sl.d_buf) cudaFree(sl.d_buf);
+    if (sl.d_info) cudaFree(sl.d_info);
+    if (sl.h_order) cudaFreeHost(sl.h_order);
+    if (sl.h_info) cudaFreeHost(sl.h_info);
+    sl.d_buf = nullptr; sl.d_info = nullptr; sl.h_order = nullptr; sl.h_info = nullptr; sl.cap = 0;
+    if (cudaMalloc((void**)&sl.d_buf, sizeof(int) * (2 * (size_t)cap + 4)) != cudaSuccess ||
+        cudaMalloc((void**)&sl.d_info, sizeof(BatchInfo) * cap) != cudaSuccess ||
+        cudaHostAlloc((void**)&sl.h_order, sizeof(int) * cap, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc((void**)&sl.h_info, sizeof(BatchInfo) * cap, cudaHostAllocDefault) != cudaSuccess)
+      return OSQP_MEM_ALLOC_ERROR;
+    sl.cap = cap;
+  }
+  if (vec > sl.vec_cap) {
+    if (sl.h_vec) cudaFreeHost(sl.h_vec);
+    sl.h_vec = nullptr; sl.vec_cap = 0;
+    const size_t want = std::max(vec, (size_t)1 << 16);
+    if (cudaHostAlloc((void**)&sl.h_vec, sizeof(T) * want, cudaHostAllocDefault) != cudaSuccess)
+      return OSQP_MEM_ALLOC_ERROR;
+    sl.vec_cap = want;
+  }
+  return 0;
+}
+
+// Issue one launch for the requests of one pool (all asynchronous on the slot's stream).
+static int slot_start(OSQPServer* S, Slot& sl, int pool, std::vector<ServeReq*>& rq) {
+  OSQPBatch* b = S->pools[pool];
+  const int k = (int)rq.size();
+  size_t vec = 0;
+  for (ServeReq* r : rq) {
+    const BatchInst& I = b->inst[r->qp];
+    vec += (size_t)I.n * 2 + (size_t)I.m * 2;
+  }
+  int rc = slot_reserve(sl, k, vec);
+  if (rc) return rc;
+  cudaStream_t st = sl.stream;
+  BatchArrays<T>& B = b->B;
+  size_t off = 0;
+  for (int i = 0; i < k; i++) {
+    ServeReq* r = rq[i];
+    const BatchInst& I = b->inst[r->qp];
+    sl.h_order[i] = r->qp;
+    auto put = [&](const std::vector<T>& v, T* dst, int len) -> int {
+      if (v.empty() || len == 0) return 0;
+      memcpy(sl.h_vec + off, v.data(), sizeof(T) * len);
+      BT_TRY(cudaMemcpyAsync(dst, sl.h_vec + off, sizeof(T) * len, cudaMemcpyHostToDevice, st));
+      off += len;
+      return 0;
+    };
+    if ((rc = put(r->q, B.vn[1] + I.n_off, I.n))) return rc;
+    if ((rc = put(r->l, B.vm[2] + I.m_off, I.m))) return rc;
+    if ((rc = put(r->u, B.vm[3] + I.m_off, I.m))) return rc;
+  }
+  int* d_order = sl.d_buf;
+  LaunchBufs lb{d_order, k, sl.d_buf + 2 * (size_t)sl.cap, sl.d_buf + sl.cap};
+  BT_TRY(cudaMemcpyAsync(d_order, sl.h_order, sizeof(int) * k, cudaMemcpyHostToDevice, st));
+  if ((rc = launch_batch(b, kModeUpdateVec, lb, st, false))) return rc;
+  if ((rc = launch_batch(b, kModeSolve, lb, st, false))) return rc;
+  k_serve_info<<<(k + 255) / 256, 256, 0, st>>>(B.st, d_order, k, sl.d_info);
+  BT_TRY(cudaGetLastError());
+  BT_TRY(cudaMemcpyAsync(sl.h_info, sl.d_info, sizeof(BatchInfo) * k, cudaMemcpyDeviceToHost, st));
+  for (int i = 0; i < k; i++) {
+    const BatchInst& I = b->inst[rq[i]->qp];
+    BT_TRY(cudaMemcpyAsync(sl.h_vec + off, B.vn[14] + I.n_off, sizeof(T) * I.n, cudaMemcpyDeviceToHost, st));
+    off += I.n;
+  }
+  BT_TRY(cudaEventRecord(sl.ev, st));
+  sl.reqs = rq;
+  sl.pool = pool;
+  sl.busy = true;
+  for (ServeReq* r : rq) S->busy[pool][r->qp] = 1;
+  return 0;
+}
+
+static void slot_finish(OSQPServer* S, Slot& sl) {
+  OSQPBatch* b = S->pools[sl.pool];
+  // x of request i follows all input vectors of the launch in the staging buffer
+  size_t off = 0;
+  for (ServeReq* r : sl.reqs) off += r->q.size() + r->l.size() + r->u.size();
+  const double t = now_s();
+  for (size_t i = 0; i < sl.reqs.size(); i++) {
+    ServeReq* r = sl.reqs[i];
+    const BatchInst& I = b->inst[r->qp];
+    r->x.assign(sl.h_vec + off, sl.h_vec + off + I.n);
+    off += I.n;
+    r->status = sl.h_info[i].status;
+    r->iter = sl.h_info[i].iter;
+    r->obj = sl.h_info[i].obj;
+    r->t1 = t;
+    r->done = true;
+    S->busy[sl.pool][r->qp] = 0;
+  }
+  sl.reqs.clear();
+  sl.busy = false;
+}
+
+static void serve_worker(OSQPServer* S) {
+  cudaSetDevice(S->device);
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    bool in_flight = false;
+    for (Slot& sl : S->slots) {
+      if (!sl.busy) continue;
+      const cudaError_t q = cudaEventQuery(sl.ev);
+      if (q == cudaErrorNotReady) { in_flight = true; continue; }
+      if (q != cudaSuccess) S->err = OSQP_ALGEBRA_LOAD_ERROR;
+      slot_finish(S, sl);
+      S->cv_done.notify_all();
+    }
+    // every free stream takes the waiting requests of the pool of the oldest
+    // one (one request per QP in flight; later ones for a busy QP wait)
+    for (Slot& sl : S->slots) {
+      if (sl.busy || S->pending.empty() || S->err) continue;
+      int pool = -1;
+      size_t cap = 0;
+      std::vector<ServeReq*> take;
+      std::vector<char> used;
+      for (auto it = S->pending.begin(); it != S->pending.end() && (pool < 0 || take.size() < cap);) {
+        ServeReq* r = *it;
+        if (pool < 0 && !S->busy[r->pool][r->qp]) {
+          pool = r->pool;
+          used.assign(S->pools[pool]->count, 0);
+          // launches hold at most the pool's resident CTA slots / streams
+          // requests, so a slow request holds back few others and new
+          // arrivals find a free stream soon
+          const int slots = S->pools[pool]->grid;   // resident QP slots (CTAs or clusters)
+          cap = (size_t)std::max(1, (slots + (int)S->slots.size() - 1) / (int)S->slots.size());
+        }
+        if (pool >= 0 && r->pool == pool && !S->busy[pool][r->qp] && !used[r->qp]) {
+          used[r->qp] = 1;
+          take.push_back(r);
+          it = S->pending.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      if (take.empty()) break;
+      if (slot_start(S, sl, pool, take)) {
+        S->err = OSQP_ALGEBRA_LOAD_ERROR;
+        for (ServeReq* r : take) { r->done = true; r->status = OSQP_UNSOLVED; }
+        S->cv_done.notify_all();
+        continue;
+      }
+      in_flight = true;
+    }
+    if (S->stop && S->pending.empty() && !in_flight) break;
+    if (in_flight) {
+      lk.unlock();
+      std::this_thread::sleep_for(std::chrono::microseconds(20));
+      lk.lock();
+    } else {
+      S->cv_work.wait(lk, [&] { return S->stop || !S->pending.empty(); });
+    }
+  }
+}
+
+extern "C" OSQPInt osqp_gb300_server_create(OSQPServer** server, OSQPInt concurrency) {
+  if (!server || concurrency < 1 || concurrency > 64) return OSQP_DATA_VALIDATION_ERROR;
+  *server = nullptr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return OSQP_ALGEBRA_LOAD_ERROR;
+  OSQPServer* S = new OSQPServer_();
+  S->device = dev;
+  S->slots.resize(concurrency);
+  for (Slot& sl : S->slots) {
+    if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
+      osqp_gb300_server_destroy(S);
+      return OSQP_ALGEBRA_LOAD_ERROR;
+    }
+  }
+  S->worker = std::thread(serve_worker, S);
+  *server = S;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_server_add_pool(OSQPServer* S, OSQPBatch* pool, OSQPInt* pool_id) {
+  if (!S || !pool || !pool_id) return OSQP_DATA_VALIDATION_ERROR;
+  if (pool->device != S->device) return OSQP_DATA_VALIDATION_ERROR;
+  std::lock_guard<std::mutex> g(S->mu);
+  S->pools.push_back(pool);
+  S->busy.emplace_back(pool->count, 0);
+  *pool_id = (OSQPInt)S->pools.size() - 1;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_server_submit(OSQPServer* S, OSQPInt pool_id, OSQPInt qp, const OSQPFloat* q,
+                                            const OSQPFloat* l, const OSQPFloat* u, long long* ticket) {
+  if (!S || !ticket) return OSQP_DATA_VALIDATION_ERROR;
+  ServeReq* r = new ServeReq();
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    if (pool_id < 0 || pool_id >= (OSQPInt)S->pools.size() || qp < 0 || qp >= S->pools[pool_id]->count) {
+      delete r;
+      return OSQP_DATA_VALIDATION_ERROR;
+    }
+    const BatchInst& I = S->pools[pool_id]->inst[qp];
+    if (q) r->q.assign(q, q + I.n);
+    if (l) r->l.assign(l, l + I.m);
+    if (u) r->u.assign(u, u + I.m);
+  }
+  if (!r->l.empty() && !r->u.empty())
+    for (size_t j = 0; j < r->l.size(); j++)
+      if (!(r->l[j] <= r->u[j])) { delete r; return OSQP_DATA_VALIDATION_ERROR; }
+  r->pool = pool_id;
+  r->qp = qp;
+  r->t0 = now_s();
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    if (S->stop) { delete r; return OSQP_WORKSPACE_NOT_INIT_ERROR; }
+    r->ticket = S->next_ticket++;
+    S->reqs[r->ticket] = r;
+    S->pending.push_back(r);
+    *ticket = r->ticket;
+  }
+  S->cv_work.notify_one();
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_server_wait(OSQPServer* S, long long ticket, OSQPFloat* x, OSQPInt* status,
+                                          OSQPInt* iter, OSQPFloat* obj_val, double* latency_ms) {
+  if (!S) return OSQP_DATA_VALIDATION_ERROR;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) return OSQP_DATA_VALIDATION_ERROR;
+  ServeReq* r = it->second;
+  S->cv_done.wait(lk, [&] { return r->done; });
+  S->reqs.erase(it);
+  lk.unlock();
+  const int err = S->err;
+  if (x && !r->x.empty()) memcpy(x, r->x.data(), sizeof(T) * r->x.size());
+  if (status) *status = r->status;
+  if (iter) *iter = r->iter;
+  if (obj_val) *obj_val = (OSQPFloat)r->obj;
+  if (latency_ms) *latency_ms = (r->t1 - r->t0) * 1e3;
+  delete r;
+  return err;
+}
+
+extern "C" OSQPInt osqp_gb300_server_destroy(OSQPServer* S) {
+  if (!S) return 0;
+  {
+    std::lock_guard<std::mutex> g(S->mu);
+    S->stop = true;
+  }
+  S->cv_work.notify_all();
+  if (S->worker.joinable()) S->worker.join();
+  cudaSetDevice(S->device);
+  for (Slot& sl : S->slots) {
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    if (sl.d_buf) cudaFree(sl.d_buf);
+    if (sl.d_info) cudaFree(sl.d_info);
+    if (sl.h_order) cudaFreeHost(sl.h_order);
+    if (sl.h_info) cudaFreeHost(sl.h_info);
+    if (sl.h_vec) cudaFreeHost(sl.h_vec);
+    if (sl.ev) cudaEventDestroy(sl.ev);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+  }
+  for (auto& kv : S->reqs) delete kv.second;
+  delete S;
   return 0;
 }

@@ -264,10 +264,7 @@ struct Solver {
   }
   template <typename G>
   __device__ void refresh_rho_vec(G& g) {
-    // local copies: hot loops keep the pointers in registers instead of
-    // re-reading them through `this` after every store
     const DevProblem<T> pr = this->pr;
-    const DevSettings s = this->s;
     SolverScalars* const sc = this->sc;
     const double rho = sc->rho;
     for_m(g, pr.m, [&](int j) {
