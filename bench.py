@@ -1,7 +1,7 @@
 """Benchmark: QP solves/s of the batched GB300 OSQP engine on batched linear MPC.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--count 4096] [--workload mpc_batch|random_qp|large_sparse]
+                    [--count 4096] [--config mpc_batch|large_sparse|svm]
 
 Workload (default, "mpc_batch"): 4096 seeded linear-MPC QPs of uneven size
 (horizon T~U{10..50}, nx~U{8..40}, nu~U{4..16}; stacked sparse OSQP form,
@@ -20,6 +20,12 @@ timed region, as an MPC controller would.
   cpu_baseline  the FP64 CPU oracle (OSQP's builtin algebra restated; direct
             LDL^T KKT solver) on the machine's host cores, process pool, over a
             bounded sample of the same QPs and steps
+
+--config large_sparse / svm run the single-QP configurations instead of the
+batch (one JSON line each, not the default line): the n=50k / m=100k sparse QP
+through the PCG path (ADMM / PCG iterations per second, achieved GB/s), and the
+m=100k x 1000 SVM at eps 1e-5 with polish (FP32 ADMM + FP64 polish, the FP64
+GPU path and the FP64 CPU oracle, objective and residual errors).
 
 --impl reference prints the CPU reference arm (the oracle port on all host
 cores) on the same workload.  With --gpus N > 1 (torchrun) every rank solves
@@ -309,6 +315,100 @@ def gpu_arm(args, probs, ls, us):
 
 
 # ---------------------------------------------------------------------------
+# Single-QP configurations
+# ---------------------------------------------------------------------------
+def _host_residuals(data, x, y):
+    import scipy.sparse as sp
+    P, q, A, l, u = data
+    Pu = P.tocsc()
+    Pf = Pu + sp.triu(Pu, 1).T
+    Ax = A @ x
+    z = np.clip(Ax, l, u)
+    prim = float(np.max(np.abs(Ax - z))) if A.shape[0] else 0.0
+    dual = float(np.max(np.abs(Pf @ x + q + A.T @ y)))
+    obj = float(0.5 * x @ (Pf @ x) + q @ x)
+    return obj, prim, dual
+
+
+def _oracle_job(args_):
+    lib_path, data, settings, linsys = args_
+    from osqp_gb300.api import Library, OSQP
+    s = OSQP(Library(lib_path, 64))
+    P, q, A, l, u = data
+    s.setup(P, q, A, pb.clip_inf(l, 1e30), pb.clip_inf(u, 1e30), linsys_solver=linsys, **settings)
+    t = time.perf_counter()
+    r = s.solve()
+    return time.perf_counter() - t, r.x, r.y, r.info["status"], r.info["iter"], r.info["status_polish"]
+
+
+def single_config(args):
+    import torch
+    from osqp_gb300 import load
+    from osqp_gb300.api import OSQP, DIRECT_SOLVER, INDIRECT_SOLVER
+    torch.cuda.set_device(0)
+    if args.config == "large_sparse":
+        data = pb.large_sparse()
+        st = dict(SETTINGS, warm_starting=0, polishing=0)
+        oracle_linsys = INDIRECT_SOLVER
+        desc = "large_sparse: n=50,000, m=100,000, P=MM'+1e-2I (8 nnz/col of M), A 10 nnz/row, eps 1e-3"
+    else:
+        data = pb.svm()
+        st = dict(SETTINGS, eps_abs=1e-5, eps_rel=1e-5, warm_starting=0, polishing=1, max_iter=20000)
+        oracle_linsys = DIRECT_SOLVER
+        desc = "svm: m=100,000 samples x 1,000 features, 15% density, lambda=1, eps 1e-5, polish"
+    P, q, A, l, u = data
+    n, m = P.shape[0], A.shape[0]
+    nnz_pf = pfull_nnz(P)
+    peak, peak_kind = measured_peak()
+    out = {"config": {"workload": desc, "n": n, "m": m, "nnz_P_full": nnz_pf, "nnz_A": int(A.nnz)},
+           "data": "synthetic (seeded)", "paths": {}}
+    for prec, inf, w in (("f32", 1e17, 4), ("f64", 1e30, 8)):
+        solver = OSQP(load(prec))
+        assert solver.setup(P, q, A, pb.clip_inf(l, inf), pb.clip_inf(u, inf), **st) == 0
+        solver.solve()                       # warm-up (cold solves: warm_starting=0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = solver.solve()
+        wall = time.perf_counter() - t
+        stt = solver.stats()
+        obj, prim, dual = _host_residuals(data, r.x, r.y)
+        kms = stt["kernel_ms"]
+        byt = solve_bytes(n, m, nnz_pf, A.nnz, w, stt["admm_iter"], stt["pcg_iter"], st["check_termination"])
+        out["paths"][prec] = {
+            "status": r.info["status"], "status_polish": r.info["status_polish"], "admm_iter": stt["admm_iter"],
+            "pcg_iter": stt["pcg_iter"], "solve_kernel_ms": kms, "solve_wall_ms": wall * 1e3,
+            "polish_ms": r.info["polish_time"] * 1e3,
+            "admm_iters_per_s": stt["admm_iter"] / (kms * 1e-3), "pcg_iters_per_s": stt["pcg_iter"] / (kms * 1e-3),
+            "execution_form": {0: "cta", 1: "grid"}.get(stt["grid"], f"cluster{stt['grid']}"),
+            "roofline": {"bound": "hbm", "achieved": byt / (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": byt / (kms * 1e-3) / 1e9 / peak, "peak_source": peak_kind},
+            "obj": obj, "prim_res": prim, "dual_res": dual}
+        solver.cleanup()
+    if args.oracle_timeout > 0:
+        lib_path = os.path.join(REPO, "oracle", "_build", "liboracle.so")
+        if not os.path.exists(lib_path):
+            subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "port"], check=True)
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(1) as pool:
+            job = pool.apply_async(_oracle_job, ((lib_path, data, st, oracle_linsys),))
+            try:
+                secs, xo, yo, status, it, spol = job.get(timeout=args.oracle_timeout)
+                obj, prim, dual = _host_residuals(data, xo, yo)
+                out["oracle"] = {"kind": "direct LDL^T (builtin)" if oracle_linsys == DIRECT_SOLVER else
+                                 "reduced-KKT PCG (FP64 restatement of the CUDA backend)", "status": status,
+                                 "iter": it, "status_polish": spol, "cpu_s": secs, "cores": 1,
+                                 "obj": obj, "prim_res": prim, "dual_res": dual}
+                for prec, pth in out["paths"].items():
+                    pth["obj_rel_err_vs_oracle"] = abs(pth["obj"] - obj) / max(1.0, abs(obj))
+            except mp.TimeoutError:
+                out["oracle"] = {"unavailable": f"FP64 CPU oracle did not finish within {args.oracle_timeout:.0f} s"}
+                pool.terminate()
+    ref = out["paths"]["f64"]["obj"]
+    out["paths"]["f32"]["obj_rel_err_vs_f64_gpu"] = abs(out["paths"]["f32"]["obj"] - ref) / max(1.0, abs(ref))
+    print(json.dumps(out))
+
+
+# ---------------------------------------------------------------------------
 # Served form: Poisson request stream over resident pools (continuous batching)
 # ---------------------------------------------------------------------------
 def serve_leg(args):
@@ -402,14 +502,20 @@ def main():
     ap.add_argument("--count", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--serve-rate", type=float, default=100.0, help="served form: Poisson arrivals (req/s); 0 = skip")
-    ap.add_argument("--serve-seconds", type=float, default=4.0)
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="served form: Poisson arrivals (req/s); 0 = skip")
+    ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--serve-streams", type=int, default=128, help="recurring problems per class")
     ap.add_argument("--serve-concurrency", type=int, default=16, help="launches in flight")
+    ap.add_argument("--config", default="mpc_batch", choices=["mpc_batch", "large_sparse", "svm"])
+    ap.add_argument("--oracle-timeout", type=float, default=900.0,
+                    help="single-QP configs: seconds allowed for the FP64 CPU oracle (0 = skip)")
     ap.add_argument("--max-iter", type=int, default=SETTINGS["max_iter"],
                     help="ADMM iteration cap (smaller values give short profiling cases)")
     args = ap.parse_args()
     SETTINGS["max_iter"] = args.max_iter
+    if args.config != "mpc_batch":
+        single_config(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     K, W = args.steps, args.warmup

@@ -662,18 +662,54 @@ template <typename G, typename FN>
 __device__ __forceinline__ void for_m(G& g, int m, FN fn) { for_rng(g, span_m(g, m), fn); }
 
 // Rows [rg.lo, rg.hi) of M, sub-warp per row (as rows_apply_L).
+// Two rows per lane group at a time: the chunk loads of both rows are issued
+// before either is used, so a warp has twice the memory requests in flight.
+// Each row's entries are still summed by the same lane in the same order.
+template <int L, typename T, typename XF>
+__device__ __forceinline__ void lane_row_dot_pair(const int* __restrict__ col, const T* __restrict__ val,
+                                                  int b0, int e0, int b1, int e1, int sl, XF xf, T& a0, T& a1) {
+  int k0 = b0 + sl, k1 = b1 + sl;
+  while (k0 < e0 || k1 < e1) {
+    int c0[kRowUnroll], c1[kRowUnroll];
+    T v0[kRowUnroll], v1[kRowUnroll];
+#pragma unroll
+    for (int u = 0; u < kRowUnroll; u++) {
+      const int ka = k0 + u * L, kb = k1 + u * L;
+      c0[u] = ka < e0 ? col[ka] : -1;
+      v0[u] = ka < e0 ? val[ka] : T(0);
+      c1[u] = kb < e1 ? col[kb] : -1;
+      v1[u] = kb < e1 ? val[kb] : T(0);
+    }
+    T x0[kRowUnroll], x1[kRowUnroll];
+#pragma unroll
+    for (int u = 0; u < kRowUnroll; u++) {
+      x0[u] = c0[u] >= 0 ? xf(c0[u]) : T(0);
+      x1[u] = c1[u] >= 0 ? xf(c1[u]) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kRowUnroll; u++) { a0 += v0[u] * x0[u]; a1 += v1[u] * x1[u]; }
+    k0 += kRowUnroll * L;
+    k1 += kRowUnroll * L;
+  }
+}
+
 template <int L, typename T, typename G, typename XF, typename FN>
 __device__ __forceinline__ void rows_rng_L(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
   const int lane = threadIdx.x & 31;
   const int sub = lane / L, sl = lane % L;
   constexpr int RPW = 32 / L;
-  const int ws = g.ws();
-  for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += ws * RPW) {
-    const int r = base + sub;
-    T acc = T(0);
-    if (r < rg.hi) acc = lane_row_dot<L>(M.col, M.val, M.rowptr[r], M.rowptr[r + 1], sl, xf);
-    acc = subwarp_sum<L>(acc);
-    if (r < rg.hi && sl == 0) fn(r, acc);
+  const int step = g.ws() * RPW;
+  for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += 2 * step) {
+    const int r0 = base + sub, r1 = base + step + sub;
+    const bool v0 = r0 < rg.hi, v1 = r1 < rg.hi;
+    const int b0 = v0 ? M.rowptr[r0] : 0, e0 = v0 ? M.rowptr[r0 + 1] : 0;
+    const int b1 = v1 ? M.rowptr[r1] : 0, e1 = v1 ? M.rowptr[r1 + 1] : 0;
+    T a0 = T(0), a1 = T(0);
+    lane_row_dot_pair<L>(M.col, M.val, b0, e0, b1, e1, sl, xf, a0, a1);
+    a0 = subwarp_sum<L>(a0);
+    a1 = subwarp_sum<L>(a1);
+    if (v0 && sl == 0) fn(r0, a0);
+    if (v1 && sl == 0) fn(r1, a1);
   }
 }
 template <typename T, typename G, typename XF, typename FN>

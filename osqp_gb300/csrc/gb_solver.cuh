@@ -118,17 +118,21 @@ __device__ __forceinline__ void kkt_rows_L(G& g, const CSR<T>& P, const CSR<T>& 
   constexpr int RPW = 32 / L;
   const Rng rg = span_n(g, P.rows);
   const int n = rg.hi;
-  const int ws = g.ws();
-  for (int base = rg.lo + g.w0() * RPW; base < n; base += ws * RPW) {
-    const int i = base + sub;
-    T a1 = T(0), a2 = T(0);
-    if (i < n) {
-      a1 = lane_row_dot<L>(P.col, P.val, P.rowptr[i], P.rowptr[i + 1], sl, xp);
-      a2 = lane_row_dot<L>(At.col, At.val, At.rowptr[i], At.rowptr[i + 1], sl, xa);
-    }
-    a1 = subwarp_sum<L>(a1);
-    a2 = subwarp_sum<L>(a2);
-    if (i < n && sl == 0) fn(i, a1, a2);
+  const int step = g.ws() * RPW;
+  // two rows per lane group at a time (gb_common.cuh lane_row_dot_pair);
+  // each row's P and A' sums keep their lane and order
+  for (int base = rg.lo + g.w0() * RPW; base < n; base += 2 * step) {
+    const int i0 = base + sub, i1 = base + step + sub;
+    const bool v0 = i0 < n, v1 = i1 < n;
+    T p0 = T(0), p1 = T(0), q0 = T(0), q1 = T(0);
+    lane_row_dot_pair<L>(P.col, P.val, v0 ? P.rowptr[i0] : 0, v0 ? P.rowptr[i0 + 1] : 0,
+                         v1 ? P.rowptr[i1] : 0, v1 ? P.rowptr[i1 + 1] : 0, sl, xp, p0, p1);
+    lane_row_dot_pair<L>(At.col, At.val, v0 ? At.rowptr[i0] : 0, v0 ? At.rowptr[i0 + 1] : 0,
+                         v1 ? At.rowptr[i1] : 0, v1 ? At.rowptr[i1 + 1] : 0, sl, xa, q0, q1);
+    p0 = subwarp_sum<L>(p0); q0 = subwarp_sum<L>(q0);
+    p1 = subwarp_sum<L>(p1); q1 = subwarp_sum<L>(q1);
+    if (v0 && sl == 0) fn(i0, p0, q0);
+    if (v1 && sl == 0) fn(i1, p1, q1);
   }
 }
 template <typename T, typename G, typename XP, typename XA, typename FN>
