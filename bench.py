@@ -190,6 +190,36 @@ def cpu_arm(probs, ls, us, sizes_m, budget_s=15.0, steps=1):
 
 
 # ---------------------------------------------------------------------------
+# Replicas (--gpus N): one process per GPU, no data-path collective; the host
+# side only synchronises the timed region and takes the slowest rank's time.
+# ---------------------------------------------------------------------------
+def replica_group(world):
+    """torch.distributed over gloo for N > 1 replicas (None for one process)."""
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
+    return dist
+
+
+def max_over_ranks(vals, dist):
+    """Element-wise maximum of a float64 vector over all ranks."""
+    vals = np.asarray(vals, dtype=np.float64)
+    if dist is None:
+        return vals
+    import torch
+    t = torch.from_numpy(vals.copy())
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.numpy()
+
+
+def whole_job_rate(units_per_rank, world, max_seconds):
+    """Units processed by all ranks over the slowest rank's time."""
+    return units_per_rank * world / max_seconds
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def gpu_arm(args, probs, ls, us):
@@ -217,10 +247,7 @@ def gpu_arm(args, probs, ls, us):
     x_out = torch.empty(b.nsum, dtype=torch.float32).pin_memory()
     torch.cuda.synchronize()
 
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
+    dist = replica_group(world)
 
     def barrier():
         if dist is not None:
@@ -273,11 +300,8 @@ def gpu_arm(args, probs, ls, us):
     e2e_s = time.perf_counter() - t0
 
     # ---- max over ranks ----
-    vals = np.array([dev_total_ms, e2e_s], dtype=np.float64)
+    vals = max_over_ranks([dev_total_ms, e2e_s], dist)
     if dist is not None:
-        t = torch.from_numpy(vals)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        vals = t.numpy()
         dist.destroy_process_group()
     dev_total_ms, e2e_s = float(vals[0]), float(vals[1])
 
@@ -300,9 +324,9 @@ def gpu_arm(args, probs, ls, us):
 
     solves = count * K * world
     out = dict(
-        value=solves / (dev_total_ms * 1e-3),
+        value=whole_job_rate(count * K, world, dev_total_ms * 1e-3),
         ms_per_step=dev_total_ms / K,
-        e2e_value=solves / e2e_s,
+        e2e_value=whole_job_rate(count * K, world, e2e_s),
         h2d=2 * 4 * int(b.msum), d2h=4 * int(b.nsum) + 40 * count,
         solve_ms=float(np.mean(solve_ms)),
         achieved_gbs=bytes_alg / K / (np.mean(solve_ms) * 1e-3) / 1e9,
