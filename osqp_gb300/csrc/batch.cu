@@ -159,27 +159,47 @@ struct Stager {
     if (dir > 0) copy(q, (const unsigned*)(rowptr + lo), hi - lo + 1);
     return (const int*)q - lo;
   }
-  // entries of rows [lo, hi); rowptr holds global positions
+  // entries of rows [lo, hi); rowptr holds global positions.  When they do
+  // not all fit, the entries of the longest prefix of rows that fits go on
+  // chip (M.scol / M.sval for rows below M.srow) and the rest stay in HBM.
   __device__ __forceinline__ void entries(CSR<TT>& M, const int* grow, int lo, int hi) {
     if (hi <= lo) return;
     const int k0 = grow[lo], k1 = grow[hi];
     if (k1 <= k0) return;
-    const int save = off;
-    unsigned* qc = take(k1 - k0);
-    unsigned* qv = qc ? take((long long)(k1 - k0) * W) : nullptr;
-    if (!qv) { off = save; return; }
-    if (dir > 0) {
-      copy(qc, (const unsigned*)(M.col + k0), k1 - k0);
-      copy(qv, (const unsigned*)(M.val + k0), (long long)(k1 - k0) * W);
+    const long long room = (long long)(cap - off) / 4 - 8;      // words, less alignment slack
+    const long long fit = room > 0 ? room / (1 + W) : 0;         // entries
+    int rs = hi;
+    if ((long long)(k1 - k0) > fit) {                             // largest rs with grow[rs] - k0 <= fit
+      int a = lo, b = hi;
+      while (a < b) {
+        const int mid = (a + b + 1) >> 1;
+        if ((long long)(grow[mid] - k0) <= fit) a = mid; else b = mid - 1;
+      }
+      rs = a;
     }
-    M.col = (const int*)qc - k0;
-    M.val = (TT*)qv - k0;
+    const int ke = grow[rs];
+    if (rs <= lo || ke <= k0) return;
+    unsigned* qc = take(ke - k0);
+    unsigned* qv = qc ? take((long long)(ke - k0) * W) : nullptr;
+    if (!qv) return;
+    if (dir > 0) {
+      copy(qc, (const unsigned*)(M.col + k0), ke - k0);
+      copy(qv, (const unsigned*)(M.val + k0), (long long)(ke - k0) * W);
+    }
+    if (rs == hi) {
+      M.col = (const int*)qc - k0;
+      M.val = (TT*)qv - k0;
+    } else {
+      M.scol = (const int*)qc - k0;
+      M.sval = (TT*)qv - k0;
+      M.srow = rs;
+    }
   }
 };
 
 template <typename TT>
 __device__ __forceinline__ bool stage_problem(DevProblem<TT>& pr, const Spans& sp, bool rho_vec,
-                                              unsigned char* base, int cap, int dir) {
+                                              unsigned char* base, int cap, int dir, bool matrices = true) {
   Stager<TT> sg{base, cap, 0, dir};
   const int n = pr.n, m = pr.m;
   const int nlo = sp.nlo, nhi = n < sp.nhi ? n : sp.nhi;
@@ -202,9 +222,11 @@ __device__ __forceinline__ bool stage_problem(DevProblem<TT>& pr, const Spans& s
   q.yv = sg.span(pr.yv, nlo, nhi, false);
   q.Kp = sg.span(pr.Kp, nlo, nhi, false);
   q.rhs = sg.span(pr.rhs, nlo, nhi, false);
-  if (m) sg.entries(q.A, growA, mlo, mhi);
-  sg.entries(q.At, growAt, nlo, nhi);
-  sg.entries(q.P, growP, nlo, nhi);
+  if (matrices) {
+    if (m) sg.entries(q.A, growA, mlo, mhi);
+    sg.entries(q.At, growAt, nlo, nhi);
+    sg.entries(q.P, growP, nlo, nhi);
+  }
   pr = q;
   return true;
 }
@@ -248,7 +270,7 @@ __device__ Spans cluster_spans(const DevProblem<TT>& pr, int kktL, int r, int c)
 template <typename TT, typename G>
 __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s, int k, int mode,
                            GroupShared& gsh, SolverScalars& ssc, unsigned char* dsm, int dsm_bytes,
-                           int it_lo, int it_hi) {
+                           int it_lo, int it_hi, bool stage_mat) {
   DevProblem<TT> pv = B.problem(k);
   if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pv.st; }
   __syncthreads();
@@ -258,7 +280,7 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
       g.sp = cluster_spans(pv, B.inst[k].kktL, (int)g.rank, (int)g.size);
       g.sliced = true;
     }
-    staged = stage_problem(pv, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, 1);
+    staged = stage_problem(pv, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, 1, stage_mat);
     if constexpr (std::is_same<G, ClusterGroup>::value) g.repl = staged;
     g.sync();   // staged copies complete in every CTA before any peer writes them
   }
@@ -288,7 +310,7 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   g.sync();
   if (staged) {
     DevProblem<TT> pb = B.problem(k);
-    stage_problem(pb, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, -1);
+    stage_problem(pb, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, -1, stage_mat);
     g.sync();   // peers may still read this CTA's copies until here
   }
   if constexpr (std::is_same<G, ClusterGroup>::value) {
@@ -308,7 +330,8 @@ struct BatchLaunch {
   const int* order;
   int mode;
   int it_lo, it_hi;   // solve window
-  int dsm_bytes;      // CTA form: dynamic shared memory for staged vectors
+  int dsm_bytes;      // dynamic shared memory for staged vectors
+  int stage_mat;      // also stage matrix entries (whole, or a prefix of rows)
 };
 
 extern __shared__ __align__(16) unsigned char g_batch_dsm[];
@@ -329,7 +352,8 @@ k_batch(BatchArrays<TT> B, DevSettings s, BatchLaunch L) {
     const int idx = s_idx;
     __syncthreads();
     if (idx >= count) break;
-    batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi);
+    batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi,
+               L.stage_mat != 0);
     if (threadIdx.x == 0) *B.problem(L.order[idx]).st = ssc;
     __syncthreads();
   }
@@ -352,7 +376,8 @@ k_batch_cluster(BatchArrays<TT> B, DevSettings s, BatchLaunch L) {
     const int idx = *cl.map_shared_rank(&gsh.cidx, 0);
     cl.sync();   // rank 0 keeps its shared memory until every CTA has read idx
     if (idx >= count) break;
-    batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi);
+    batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi,
+               L.stage_mat != 0);
     if (g.rank == 0 && threadIdx.x == 0) *B.problem(L.order[idx]).st = ssc;
     cl.sync();
   }
@@ -562,6 +587,7 @@ struct OSQPBatch_ {
   int split;              // ADMM iteration after which unfinished QPs move to the tail form (0: never)
   int tail_cluster, tail_grid;   // tail form: CTAs per QP and resident clusters
   int *d_order2, *d_count2, *d_queue2;
+  int stage_mat;          // stage matrix entries on chip when they (partly) fit
   float last_ms, last_step_ms;
   long long last_admm, last_pcg;
   std::vector<BatchInst> inst;
@@ -607,7 +633,7 @@ static int launch_batch(OSQPBatch* b, int mode, const LaunchBufs& lb, cudaStream
   int* q2 = lb.queue + 1;
   int* c2 = lb.queue + 2;
   BT_TRY(cudaMemsetAsync(lb.queue, 0, 3 * sizeof(int), st));
-  BatchLaunch L{lb.count, nullptr, q1, lb.order, mode, 1, 0x7fffffff, 0};
+  BatchLaunch L{lb.count, nullptr, q1, lb.order, mode, 1, 0x7fffffff, 0, b->stage_mat};
   const bool split = allow_split && mode == kModeSolve && b->split > 0 && b->split < b->ds.max_iter &&
                      b->cluster < b->tail_cluster;
   if (split) L.it_hi = b->split;
@@ -625,7 +651,7 @@ static int launch_batch(OSQPBatch* b, int mode, const LaunchBufs& lb, cudaStream
     // stopped, with a cluster of CTAs each: the slowest QPs set the makespan
     k_batch_unfinished<<<1, 1024, 0, st>>>(b->B.st, lb.order, lb.count, lb.order2, c2);
     BT_TRY(cudaGetLastError());
-    BatchLaunch T2{0, c2, q2, lb.order2, kModeSolve, b->split + 1, 0x7fffffff, 0};
+    BatchLaunch T2{0, c2, q2, lb.order2, kModeSolve, b->split + 1, 0x7fffffff, 0, b->stage_mat};
     const int tgrid = std::max(1, std::min(lb.count, b->tail_grid));
     if (b->tail_cluster >= 1) {
       T2.dsm_bytes = b->cdsm;
@@ -883,6 +909,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   // per QP with staged vectors, and QPs still running after 1000 ADMM
   // iterations continue on 8-CTA clusters with the QP in shared memory.
   b->split = std::max(0, env_int("OSQP_GB300_BATCH_SPLIT", 1000));
+  b->stage_mat = env_int("OSQP_GB300_BATCH_STAGE_MATRIX", 1) != 0;
   b->tail_cluster = std::max(0, std::min(16, env_int("OSQP_GB300_BATCH_TAIL", 8)));
   b->tail_grid = 0;
   while (b->split > 0 && b->tail_cluster >= 1) {

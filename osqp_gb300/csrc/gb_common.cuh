@@ -519,6 +519,13 @@ struct CSR {
   int rows;
   int cols;
   int lanes;  // lanes per row: 1,2,4,8,16,32
+  // optional on-chip copy of the entries of rows [.., srow): scol / sval are
+  // addressed by the same positions as col / val (the sparse-product loops
+  // read them for rows below srow; everything else may keep reading col / val,
+  // which hold the same values)
+  const int* scol = nullptr;
+  T* sval = nullptr;
+  int srow = 0;
 };
 
 
@@ -666,8 +673,9 @@ __device__ __forceinline__ void for_m(G& g, int m, FN fn) { for_rng(g, span_m(g,
 // before either is used, so a warp has twice the memory requests in flight.
 // Each row's entries are still summed by the same lane in the same order.
 template <int L, typename T, typename XF>
-__device__ __forceinline__ void lane_row_dot_pair(const int* __restrict__ col, const T* __restrict__ val,
-                                                  int b0, int e0, int b1, int e1, int sl, XF xf, T& a0, T& a1) {
+__device__ __forceinline__ void lane_row_dot_pair(const int* col0, const T* val0, int b0, int e0,
+                                                  const int* col1, const T* val1, int b1, int e1, int sl,
+                                                  XF xf, T& a0, T& a1) {
   int k0 = b0 + sl, k1 = b1 + sl;
   while (k0 < e0 || k1 < e1) {
     int c0[kRowUnroll], c1[kRowUnroll];
@@ -675,10 +683,10 @@ __device__ __forceinline__ void lane_row_dot_pair(const int* __restrict__ col, c
 #pragma unroll
     for (int u = 0; u < kRowUnroll; u++) {
       const int ka = k0 + u * L, kb = k1 + u * L;
-      c0[u] = ka < e0 ? col[ka] : -1;
-      v0[u] = ka < e0 ? val[ka] : T(0);
-      c1[u] = kb < e1 ? col[kb] : -1;
-      v1[u] = kb < e1 ? val[kb] : T(0);
+      c0[u] = ka < e0 ? col0[ka] : -1;
+      v0[u] = ka < e0 ? val0[ka] : T(0);
+      c1[u] = kb < e1 ? col1[kb] : -1;
+      v1[u] = kb < e1 ? val1[kb] : T(0);
     }
     T x0[kRowUnroll], x1[kRowUnroll];
 #pragma unroll
@@ -705,7 +713,9 @@ __device__ __forceinline__ void rows_rng_L(G& g, Rng rg, const CSR<T>& M, XF xf,
     const int b0 = v0 ? M.rowptr[r0] : 0, e0 = v0 ? M.rowptr[r0 + 1] : 0;
     const int b1 = v1 ? M.rowptr[r1] : 0, e1 = v1 ? M.rowptr[r1 + 1] : 0;
     T a0 = T(0), a1 = T(0);
-    lane_row_dot_pair<L>(M.col, M.val, b0, e0, b1, e1, sl, xf, a0, a1);
+    const bool s0 = r0 < M.srow, s1 = r1 < M.srow;
+    lane_row_dot_pair<L>(s0 ? M.scol : M.col, s0 ? M.sval : M.val, b0, e0,
+                         s1 ? M.scol : M.col, s1 ? M.sval : M.val, b1, e1, sl, xf, a0, a1);
     a0 = subwarp_sum<L>(a0);
     a1 = subwarp_sum<L>(a1);
     if (v0 && sl == 0) fn(r0, a0);

@@ -125,9 +125,12 @@ __device__ __forceinline__ void kkt_rows_L(G& g, const CSR<T>& P, const CSR<T>& 
     const int i0 = base + sub, i1 = base + step + sub;
     const bool v0 = i0 < n, v1 = i1 < n;
     T p0 = T(0), p1 = T(0), q0 = T(0), q1 = T(0);
-    lane_row_dot_pair<L>(P.col, P.val, v0 ? P.rowptr[i0] : 0, v0 ? P.rowptr[i0 + 1] : 0,
+    const bool sp0 = i0 < P.srow, sp1 = i1 < P.srow, sa0 = i0 < At.srow, sa1 = i1 < At.srow;
+    lane_row_dot_pair<L>(sp0 ? P.scol : P.col, sp0 ? P.sval : P.val, v0 ? P.rowptr[i0] : 0,
+                         v0 ? P.rowptr[i0 + 1] : 0, sp1 ? P.scol : P.col, sp1 ? P.sval : P.val,
                          v1 ? P.rowptr[i1] : 0, v1 ? P.rowptr[i1 + 1] : 0, sl, xp, p0, p1);
-    lane_row_dot_pair<L>(At.col, At.val, v0 ? At.rowptr[i0] : 0, v0 ? At.rowptr[i0 + 1] : 0,
+    lane_row_dot_pair<L>(sa0 ? At.scol : At.col, sa0 ? At.sval : At.val, v0 ? At.rowptr[i0] : 0,
+                         v0 ? At.rowptr[i0 + 1] : 0, sa1 ? At.scol : At.col, sa1 ? At.sval : At.val,
                          v1 ? At.rowptr[i1] : 0, v1 ? At.rowptr[i1 + 1] : 0, sl, xa, q0, q1);
     p0 = subwarp_sum<L>(p0); q0 = subwarp_sum<L>(q0);
     p1 = subwarp_sum<L>(p1); q1 = subwarp_sum<L>(q1);
