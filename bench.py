@@ -78,6 +78,14 @@ def make_workload(count, steps, seed=3):
     return probs, ls, us
 
 
+# DRAM bytes per algorithmic byte of the CTA-form solve launch, from the ncu
+# capture of 304 batched MPC QPs (profiles/k_batch_solve_mpc304.md:
+# 67.3 + 8.3 GB DRAM for 285.6 GB algorithmic).  The 4096-QP launch is too
+# long to capture under the size rule; its traffic is this ratio times its
+# algorithmic bytes (the matrices of the QPs in flight stay L2-resident in both).
+TRAFFIC_PER_ALGORITHMIC_BYTE = (67.304107 + 8.307210) / 285.586664900
+
+
 def measured_peak():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     try:
@@ -589,7 +597,10 @@ def main():
         e2e={"value": g["e2e_value"], "unit": "solves/s", "h2d_bytes_per_step": g["h2d"],
              "d2h_bytes_per_step": g["d2h"]},
         roofline={"bound": "hbm", "achieved": g["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                  "frac": g["achieved_gbs"] / peak, "traffic": None,
+                  "frac": g["achieved_gbs"] / peak,
+                  "traffic": TRAFFIC_PER_ALGORITHMIC_BYTE * g["bytes_per_launch"],
+                  "traffic_source": "ncu capture of 304 QPs (dram read+write / algorithmic bytes = "
+                                    f"{TRAFFIC_PER_ALGORITHMIC_BYTE:.3f}) scaled to this launch's algorithmic bytes",
                   "kernel": "k_batch (solve)", "peak_source": peak_kind,
                   "algorithmic_bytes_per_launch": g["bytes_per_launch"], "kernel_ms": g["solve_ms"]},
         cpu_baseline=None if not cpu else {"value": cpu["value"], "unit": "solves/s", "cores": cpu["cores"],
