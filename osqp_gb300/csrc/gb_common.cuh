@@ -535,9 +535,10 @@ struct CSR {
 // Entries per lane loaded before any is used: the index/value loads of a
 // chunk are independent, so a row costs ceil(len / (kRowUnroll * L)) memory
 // latencies.  The summation order (k ascending per lane) does not depend on
-// it.  (8 measured slower than 4 on batched MPC: more predicated work on the
-// many short rows.)
-constexpr int kRowUnroll = 4;
+// it.  Measured on batched MPC (one box, alternating builds): 2 -> 502,
+// 4 -> 426, 8 -> 270 solves/s; short rows waste the predicated slots of a
+// long unroll, and two rows in flight already cover the latency.
+constexpr int kRowUnroll = 2;
 
 template <int L, typename T, typename XF>
 __device__ __forceinline__ T lane_row_dot(const int* __restrict__ col, const T* __restrict__ val,
