@@ -244,6 +244,7 @@ def gpu_arm(args, probs, ls, us):
     b = Batch(lib)
     rc = b.setup(probs, **settings)
     assert rc == 0, f"batch setup failed: {rc}"
+    tile = b.autotune(30)      # SpMV tile (entries per lane), timed on a sample; state restored
     count = b.count
     K, W = args.steps, args.warmup
     nsteps = K + W
@@ -341,7 +342,7 @@ def gpu_arm(args, probs, ls, us):
         bytes_per_launch=bytes_alg / K,
         admm_per_qp=admm_tot / (count * K), pcg_per_qp=pcg_tot / (count * K),
         status_counts={int(k): int(v) for k, v in zip(*np.unique(status_last, return_counts=True))},
-        obj_last=obj_first, launches=launches, clocks=clk, plain=plain, rank=rank, world=world,
+        obj_last=obj_first, launches=launches, clocks=clk, plain=plain, rank=rank, world=world, tile=tile,
     )
     return out
 
@@ -610,6 +611,7 @@ def main():
         batched_over_plain=(g["value"] / g["plain"]) if g["plain"] else None,
         admm_iters_per_qp=g["admm_per_qp"], pcg_iters_per_qp=g["pcg_per_qp"],
         status_counts=g["status_counts"], objective_vs_fp64_oracle=obj_err,
+        spmv_tile_entries_per_lane=g["tile"],
         served=served,
     )
     print(json.dumps(line))

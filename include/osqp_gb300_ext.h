@@ -60,6 +60,15 @@ OSQPInt osqp_gb300_batch_get_solution(OSQPBatch* batch, OSQPFloat* x, OSQPFloat*
                                       OSQPInt* iter, OSQPFloat* obj_val, OSQPFloat* prim_res,
                                       OSQPFloat* dual_res);
 
+/* SpMV tile autotuner: times a short solve (probe_iter ADMM iterations; <= 0
+ * means 30) of a sample of the batch for several targets of matrix entries
+ * per lane of a row's sub-warp, keeps the fastest for every later solve and
+ * returns it in *per_lane (may be NULL).  Every iterate and scalar of the
+ * batch is restored afterwards.  The tile changes the summation order inside
+ * a row, so results are reproducible for a given tile; the default tile
+ * (OSQP_GB300_LANE_TARGET, 8) does not depend on the batch. */
+OSQPInt osqp_gb300_batch_autotune(OSQPBatch* batch, OSQPInt probe_iter, OSQPInt* per_lane);
+
 /* Device time of the last batch solve (ms), total ADMM and PCG iterations. */
 OSQPInt osqp_gb300_batch_stats(OSQPBatch* batch, double* kernel_ms, long long* admm_iter,
                                long long* pcg_iter);

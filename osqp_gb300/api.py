@@ -324,6 +324,8 @@ class Batch:
         L.osqp_gb300_batch_pcg_iters.restype = I
         L.osqp_gb300_batch_cleanup.argtypes = [C.c_void_p]
         L.osqp_gb300_batch_cleanup.restype = I
+        L.osqp_gb300_batch_autotune.argtypes = [C.c_void_p, I, C.POINTER(I)]
+        L.osqp_gb300_batch_autotune.restype = I
 
     @staticmethod
     def pack(problems, float_dtype):
@@ -420,6 +422,14 @@ class Batch:
         ms, a, p = C.c_double(), C.c_longlong(), C.c_longlong()
         self.L.lib.osqp_gb300_batch_stats(self._h, C.byref(ms), C.byref(a), C.byref(p))
         return {"kernel_ms": ms.value, "admm_iter": a.value, "pcg_iter": p.value}
+
+    def autotune(self, probe_iter: int = 30) -> int:
+        """Pick the SpMV tile (entries per lane) by timing; returns it."""
+        v = self.L.I()
+        rc = self.L.lib.osqp_gb300_batch_autotune(self._h, probe_iter, C.byref(v))
+        if rc:
+            raise RuntimeError(f"osqp_gb300_batch_autotune failed: {rc}")
+        return int(v.value)
 
     def cleanup(self):
         if self._h:

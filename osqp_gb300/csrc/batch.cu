@@ -555,6 +555,15 @@ static int configure_dsm(BatchKernel fn, int threads, int minb, int device, long
   return (int)std::max(per_cta, 0L);
 }
 
+// SpMV tile of every QP: lanes per row for P, A, A' and the fused P / A'
+// pass, from the mean row length and the target entries per lane.  The
+// default target was measured on batched MPC (one box, alternating): 1 -> 315,
+// 2 -> 401, 4 -> 521, 8 -> 546, 16 -> 430, 32 -> 260 solves/s;
+// osqp_gb300_batch_autotune picks it per batch by timing.
+constexpr int kDefaultPerLane = 8;
+
+static void assign_lanes(OSQPBatch_* b, int per_lane);
+
 static int env_int(const char* name, int dflt) {
   const char* e = getenv(name);
   return (e && *e) ? atoi(e) : dflt;
@@ -588,10 +597,26 @@ struct OSQPBatch_ {
   int tail_cluster, tail_grid;   // tail form: CTAs per QP and resident clusters
   int *d_order2, *d_count2, *d_queue2;
   int stage_mat;          // stage matrix entries on chip when they (partly) fit
+  int per_lane;           // SpMV tile: target entries per lane of a row's sub-warp
+  std::vector<long long> nnzT_k, nnzA_k;   // per QP: entries of triu(P) and of A
+  std::vector<int> order_h;                 // host copy of the queue order
   float last_ms, last_step_ms;
   long long last_admm, last_pcg;
   std::vector<BatchInst> inst;
 };
+
+static void assign_lanes(OSQPBatch_* b, int per_lane) {
+  for (int k = 0; k < b->count; k++) {
+    BatchInst& I = b->inst[k];
+    const long long nPf_est = 2 * b->nnzT_k[k] + I.n;   // lane choice only needs the mean row length
+    const long long nA = b->nnzA_k[k];
+    I.PL = pick_lanes(nPf_est, I.n, per_lane);
+    I.AL = pick_lanes(nA, I.m, per_lane);
+    I.AtL = pick_lanes(nA, I.n, per_lane);
+    I.kktL = pick_lanes(nPf_est + nA, I.n, per_lane);
+  }
+  b->per_lane = per_lane;
+}
 
 // settings translation shared with the single-QP engine
 static DevSettings batch_dev_settings(const OSQPSettings* st) {
@@ -628,7 +653,10 @@ struct LaunchBufs {
 // allow_split = false keeps every QP of the launch in the first form: a
 // serving launch must not wait for a whole cluster of idle SMs while other
 // launches occupy the GPU.
-static int launch_batch(OSQPBatch* b, int mode, const LaunchBufs& lb, cudaStream_t st, bool allow_split = true) {
+// it_stop > 0: stop every QP after that many ADMM iterations (suspended, as
+// at a split, but without a tail launch).
+static int launch_batch(OSQPBatch* b, int mode, const LaunchBufs& lb, cudaStream_t st, bool allow_split = true,
+                        int it_stop = 0) {
   int* q1 = lb.queue;
   int* q2 = lb.queue + 1;
   int* c2 = lb.queue + 2;
@@ -637,6 +665,7 @@ static int launch_batch(OSQPBatch* b, int mode, const LaunchBufs& lb, cudaStream
   const bool split = allow_split && mode == kModeSolve && b->split > 0 && b->split < b->ds.max_iter &&
                      b->cluster < b->tail_cluster;
   if (split) L.it_hi = b->split;
+  if (it_stop > 0 && !split) L.it_hi = it_stop;
   const int grid = std::max(1, std::min(lb.count, b->grid));   // a small launch leaves SMs to others
   if (b->cluster >= 1) {
     L.dsm_bytes = mode == kModeSolve ? b->cdsm : 0;
@@ -753,17 +782,15 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     }
   }
   b->nnzPf = 2 * pto - 2 * ndiag + nsum;
+  b->nnzT_k.resize(count); b->nnzA_k.resize(count);
   for (int k = 0; k < count; k++) {
-    BatchInst& I = b->inst[k];
     const OSQPInt* P = hPp.data() + pp_off[k];
     const OSQPInt* A = hAp.data() + pp_off[k];
-    const long long nT = P[I.n], nA = A[I.n];
-    long long nPf_est = 2 * nT + I.n;  // lane choice only needs the mean row length
-    I.PL = pick_lanes(nPf_est, I.n);
-    I.AL = pick_lanes(nA, I.m);
-    I.AtL = pick_lanes(nA, I.n);
-    I.kktL = pick_lanes(nPf_est + nA, I.n);
+    b->nnzT_k[k] = P[b->inst[k].n];
+    b->nnzA_k[k] = A[b->inst[k].n];
   }
+  b->per_lane = std::max(1, std::min(64, env_int("OSQP_GB300_LANE_TARGET", kDefaultPerLane)));
+  assign_lanes(b, b->per_lane);
   std::vector<int> order(count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return work[a] > work[c]; });
@@ -820,6 +847,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
 
   BT_TRY(cudaMemcpyAsync(b->d_inst, b->inst.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice, s));
   BT_TRY(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
+  b->order_h = order;
   BT_TRY(cudaMemcpyAsync(B.Praw, Px, sizeof(T) * pto, cudaMemcpyDefault, s));
   BT_TRY(cudaMemcpyAsync(B.Araw, Ax, sizeof(T) * ao, cudaMemcpyDefault, s));
   BT_TRY(cudaMemcpyAsync(B.vn[1], q, sizeof(T) * nsum, cudaMemcpyDefault, s));
@@ -971,6 +999,76 @@ extern "C" OSQPInt osqp_gb300_batch_solve(OSQPBatch* b) {
   b->upd_pending = 0;
   b->last_admm = tot[0]; b->last_pcg = tot[1];
   return 0;
+}
+
+// SpMV tile autotuner: time a short windowed solve (probe_iter ADMM iterations,
+// one QP per resident CTA, sampled evenly along the queue) for each candidate
+// target of entries per lane, keep the fastest, and put every iterate and
+// scalar back as it was.
+extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, OSQPInt* per_lane) {
+  if (!b) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  cudaSetDevice(b->device);
+  cudaStream_t s = b->stream;
+  const int probe = std::max(1, std::min((int)(probe_iter > 0 ? probe_iter : 30), b->ds.max_iter));
+  const int ns = std::max(1, std::min(b->count, b->grid));   // one QP per resident CTA / cluster
+  std::vector<int> sample(ns);
+  for (int i = 0; i < ns; i++) sample[i] = b->order_h[(long long)i * b->count / ns];
+  BatchArrays<T>& B = b->B;
+  const size_t vbytes = sizeof(T) * 16 * (size_t)(b->nsum + b->msum);
+  const size_t sbytes = sizeof(SolverScalars) * (size_t)b->count;
+  char* snap = nullptr;
+  int* dbuf = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = 0;
+  int best = b->per_lane;
+  if (cudaMallocAsync((void**)&snap, vbytes + sbytes, s) != cudaSuccess ||
+      cudaMallocAsync((void**)&dbuf, sizeof(int) * (2 * (size_t)ns + 4), s) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = OSQP_MEM_ALLOC_ERROR;
+  size_t off = 0;
+  for (int k = 0; !rc && k < 16; k++) {
+    cudaMemcpyAsync(snap + off, B.vn[k], sizeof(T) * b->nsum, cudaMemcpyDeviceToDevice, s); off += sizeof(T) * b->nsum;
+    cudaMemcpyAsync(snap + off, B.vm[k], sizeof(T) * b->msum, cudaMemcpyDeviceToDevice, s); off += sizeof(T) * b->msum;
+  }
+  if (!rc) cudaMemcpyAsync(snap + off, B.st, sbytes, cudaMemcpyDeviceToDevice, s);
+  if (!rc) cudaMemcpyAsync(dbuf, sample.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s);
+  LaunchBufs lb{dbuf, ns, dbuf + 2 * (size_t)ns, dbuf + ns};
+  float best_ms = 1e30f;
+  for (int cand : {4, 8, 16}) {
+    if (rc) break;
+    assign_lanes(b, cand);
+    cudaMemcpyAsync(b->d_inst, b->inst.data(), sizeof(BatchInst) * b->count, cudaMemcpyHostToDevice, s);
+    float ms = 1e30f;
+    for (int rep = 0; rep < 2 && !rc; rep++) {
+      // back to the saved state, then a solve of the sample stopped after `probe` iterations
+      cudaMemcpyAsync(B.st, snap + off, sbytes, cudaMemcpyDeviceToDevice, s);
+      cudaEventRecord(e0, s);
+      if (launch_batch(b, kModeSolve, lb, s, false, probe)) rc = OSQP_ALGEBRA_LOAD_ERROR;
+      cudaEventRecord(e1, s);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = OSQP_ALGEBRA_LOAD_ERROR;
+      float t = 0.f;
+      cudaEventElapsedTime(&t, e0, e1);
+      ms = std::min(ms, t);
+    }
+    if (ms < best_ms) { best_ms = ms; best = cand; }
+  }
+  // the chosen tile, and every vector and scalar as before the probes
+  assign_lanes(b, best);
+  cudaMemcpyAsync(b->d_inst, b->inst.data(), sizeof(BatchInst) * b->count, cudaMemcpyHostToDevice, s);
+  if (snap) {
+    off = 0;
+    for (int k = 0; k < 16; k++) {
+      cudaMemcpyAsync(B.vn[k], snap + off, sizeof(T) * b->nsum, cudaMemcpyDeviceToDevice, s); off += sizeof(T) * b->nsum;
+      cudaMemcpyAsync(B.vm[k], snap + off, sizeof(T) * b->msum, cudaMemcpyDeviceToDevice, s); off += sizeof(T) * b->msum;
+    }
+    cudaMemcpyAsync(B.st, snap + off, sbytes, cudaMemcpyDeviceToDevice, s);
+    cudaFreeAsync(snap, s);
+  }
+  if (dbuf) cudaFreeAsync(dbuf, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) rc = OSQP_ALGEBRA_LOAD_ERROR;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (per_lane) *per_lane = best;
+  return rc;
 }
 
 extern "C" OSQPInt osqp_gb300_batch_get_solution(OSQPBatch* b, OSQPFloat* x, OSQPFloat* y, OSQPInt* status,

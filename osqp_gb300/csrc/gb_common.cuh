@@ -535,10 +535,11 @@ struct CSR {
 // Entries per lane loaded before any is used: the index/value loads of a
 // chunk are independent, so a row costs ceil(len / (kRowUnroll * L)) memory
 // latencies.  The summation order (k ascending per lane) does not depend on
-// it.  Measured on batched MPC (one box, alternating builds): 2 -> 502,
-// 4 -> 426, 8 -> 270 solves/s; short rows waste the predicated slots of a
-// long unroll, and two rows in flight already cover the latency.
-constexpr int kRowUnroll = 2;
+// it.  Measured on batched MPC (one box, alternating builds), with
+// kRowsInFlight rows per lane group: (rows, unroll) = (2, 1) 523, (2, 2) 505,
+// (4, 1) 491, (4, 2) 395, (2, 4) 426, (2, 8) 270 solves/s; short rows waste
+// the predicated slots of a long unroll, and the kernel is issue-limited.
+constexpr int kRowUnroll = 1;
 
 template <int L, typename T, typename XF>
 __device__ __forceinline__ T lane_row_dot(const int* __restrict__ col, const T* __restrict__ val,
@@ -646,11 +647,11 @@ __device__ __forceinline__ void rows_apply2(G& g, const CSR<T>& M, XF1 a, XF2 b,
 
 // Lanes per row from the mean row length: about four entries per lane
 // (power of two, 1..32), so short rows pack several rows into a warp.
-inline int pick_lanes(long long nnz, int rows) {
+inline int pick_lanes(long long nnz, int rows, int per_lane = 4) {
   if (rows <= 0) return 1;
   const double mean = (double)nnz / rows;
   int L = 1;
-  while (L < 32 && L * 4 < mean) L <<= 1;
+  while (L < 32 && L * per_lane < mean) L <<= 1;
   return L;
 }
 
@@ -670,57 +671,82 @@ template <typename G, typename FN>
 __device__ __forceinline__ void for_m(G& g, int m, FN fn) { for_rng(g, span_m(g, m), fn); }
 
 // Rows [rg.lo, rg.hi) of M, sub-warp per row (as rows_apply_L).
-// Two rows per lane group at a time: the chunk loads of both rows are issued
-// before either is used, so a warp has twice the memory requests in flight.
-// Each row's entries are still summed by the same lane in the same order.
-template <int L, typename T, typename XF>
-__device__ __forceinline__ void lane_row_dot_pair(const int* col0, const T* val0, int b0, int e0,
-                                                  const int* col1, const T* val1, int b1, int e1, int sl,
-                                                  XF xf, T& a0, T& a1) {
-  int k0 = b0 + sl, k1 = b1 + sl;
-  while (k0 < e0 || k1 < e1) {
-    int c0[kRowUnroll], c1[kRowUnroll];
-    T v0[kRowUnroll], v1[kRowUnroll];
+// Rows in flight per lane group: the chunk loads of all of them are issued
+// before any is used, so a warp has kRowsInFlight times the memory requests
+// in flight.  Each row's entries are still summed by the same lane in the
+// same order.
+constexpr int kRowsInFlight = 2;
+
+template <int L, int NR, typename T, typename XF>
+__device__ __forceinline__ void lane_rows_dot(const int* const (&col)[NR], const T* const (&val)[NR],
+                                              const int (&b)[NR], const int (&e)[NR], int sl, XF xf,
+                                              T (&acc)[NR]) {
+  int k[NR];
+  bool more = false;
 #pragma unroll
-    for (int u = 0; u < kRowUnroll; u++) {
-      const int ka = k0 + u * L, kb = k1 + u * L;
-      c0[u] = ka < e0 ? col0[ka] : -1;
-      v0[u] = ka < e0 ? val0[ka] : T(0);
-      c1[u] = kb < e1 ? col1[kb] : -1;
-      v1[u] = kb < e1 ? val1[kb] : T(0);
+  for (int r = 0; r < NR; r++) { k[r] = b[r] + sl; more |= k[r] < e[r]; }
+  while (more) {
+    int c[NR][kRowUnroll];
+    T v[NR][kRowUnroll];
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+#pragma unroll
+      for (int u = 0; u < kRowUnroll; u++) {
+        const int kk = k[r] + u * L;
+        c[r][u] = kk < e[r] ? col[r][kk] : -1;
+        v[r][u] = kk < e[r] ? val[r][kk] : T(0);
+      }
+    T x[NR][kRowUnroll];
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+#pragma unroll
+      for (int u = 0; u < kRowUnroll; u++) x[r][u] = c[r][u] >= 0 ? xf(c[r][u]) : T(0);
+    more = false;
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+#pragma unroll
+      for (int u = 0; u < kRowUnroll; u++) acc[r] += v[r][u] * x[r][u];
+      k[r] += kRowUnroll * L;
+      more |= k[r] < e[r];
     }
-    T x0[kRowUnroll], x1[kRowUnroll];
-#pragma unroll
-    for (int u = 0; u < kRowUnroll; u++) {
-      x0[u] = c0[u] >= 0 ? xf(c0[u]) : T(0);
-      x1[u] = c1[u] >= 0 ? xf(c1[u]) : T(0);
-    }
-#pragma unroll
-    for (int u = 0; u < kRowUnroll; u++) { a0 += v0[u] * x0[u]; a1 += v1[u] * x1[u]; }
-    k0 += kRowUnroll * L;
-    k1 += kRowUnroll * L;
   }
+}
+
+// Row r's entry pointers: the on-chip copy below M.srow, else HBM.
+template <typename T>
+__device__ __forceinline__ void row_ptrs(const CSR<T>& M, int r, bool valid, const int*& col, const T*& val,
+                                         int& b, int& e) {
+  const bool s = r < M.srow;
+  col = s ? M.scol : M.col;
+  val = s ? M.sval : M.val;
+  b = valid ? M.rowptr[r] : 0;
+  e = valid ? M.rowptr[r + 1] : 0;
 }
 
 template <int L, typename T, typename G, typename XF, typename FN>
 __device__ __forceinline__ void rows_rng_L(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
+  constexpr int NR = kRowsInFlight;
   const int lane = threadIdx.x & 31;
   const int sub = lane / L, sl = lane % L;
   constexpr int RPW = 32 / L;
   const int step = g.ws() * RPW;
-  for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += 2 * step) {
-    const int r0 = base + sub, r1 = base + step + sub;
-    const bool v0 = r0 < rg.hi, v1 = r1 < rg.hi;
-    const int b0 = v0 ? M.rowptr[r0] : 0, e0 = v0 ? M.rowptr[r0 + 1] : 0;
-    const int b1 = v1 ? M.rowptr[r1] : 0, e1 = v1 ? M.rowptr[r1 + 1] : 0;
-    T a0 = T(0), a1 = T(0);
-    const bool s0 = r0 < M.srow, s1 = r1 < M.srow;
-    lane_row_dot_pair<L>(s0 ? M.scol : M.col, s0 ? M.sval : M.val, b0, e0,
-                         s1 ? M.scol : M.col, s1 ? M.sval : M.val, b1, e1, sl, xf, a0, a1);
-    a0 = subwarp_sum<L>(a0);
-    a1 = subwarp_sum<L>(a1);
-    if (v0 && sl == 0) fn(r0, a0);
-    if (v1 && sl == 0) fn(r1, a1);
+  for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += NR * step) {
+    const int* col[NR];
+    const T* val[NR];
+    int b[NR], e[NR];
+    T acc[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      row_ptrs(M, base + r * step + sub, base + r * step + sub < rg.hi, col[r], val[r], b[r], e[r]);
+      acc[r] = T(0);
+    }
+    lane_rows_dot<L, NR>(col, val, b, e, sl, xf, acc);
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      const T a = subwarp_sum<L>(acc[r]);
+      const int row = base + r * step + sub;
+      if (row < rg.hi && sl == 0) fn(row, a);
+    }
   }
 }
 template <typename T, typename G, typename XF, typename FN>

@@ -119,23 +119,28 @@ __device__ __forceinline__ void kkt_rows_L(G& g, const CSR<T>& P, const CSR<T>& 
   const Rng rg = span_n(g, P.rows);
   const int n = rg.hi;
   const int step = g.ws() * RPW;
-  // two rows per lane group at a time (gb_common.cuh lane_row_dot_pair);
+  constexpr int NR = kRowsInFlight;
+  // several rows per lane group at a time (gb_common.cuh lane_rows_dot);
   // each row's P and A' sums keep their lane and order
-  for (int base = rg.lo + g.w0() * RPW; base < n; base += 2 * step) {
-    const int i0 = base + sub, i1 = base + step + sub;
-    const bool v0 = i0 < n, v1 = i1 < n;
-    T p0 = T(0), p1 = T(0), q0 = T(0), q1 = T(0);
-    const bool sp0 = i0 < P.srow, sp1 = i1 < P.srow, sa0 = i0 < At.srow, sa1 = i1 < At.srow;
-    lane_row_dot_pair<L>(sp0 ? P.scol : P.col, sp0 ? P.sval : P.val, v0 ? P.rowptr[i0] : 0,
-                         v0 ? P.rowptr[i0 + 1] : 0, sp1 ? P.scol : P.col, sp1 ? P.sval : P.val,
-                         v1 ? P.rowptr[i1] : 0, v1 ? P.rowptr[i1 + 1] : 0, sl, xp, p0, p1);
-    lane_row_dot_pair<L>(sa0 ? At.scol : At.col, sa0 ? At.sval : At.val, v0 ? At.rowptr[i0] : 0,
-                         v0 ? At.rowptr[i0 + 1] : 0, sa1 ? At.scol : At.col, sa1 ? At.sval : At.val,
-                         v1 ? At.rowptr[i1] : 0, v1 ? At.rowptr[i1 + 1] : 0, sl, xa, q0, q1);
-    p0 = subwarp_sum<L>(p0); q0 = subwarp_sum<L>(q0);
-    p1 = subwarp_sum<L>(p1); q1 = subwarp_sum<L>(q1);
-    if (v0 && sl == 0) fn(i0, p0, q0);
-    if (v1 && sl == 0) fn(i1, p1, q1);
+  for (int base = rg.lo + g.w0() * RPW; base < n; base += NR * step) {
+    const int* pc[NR]; const T* pv[NR]; int pb[NR], pe[NR];
+    const int* ac[NR]; const T* av[NR]; int ab[NR], ae[NR];
+    T ps[NR], as[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      const int i = base + r * step + sub;
+      row_ptrs(P, i, i < n, pc[r], pv[r], pb[r], pe[r]);
+      row_ptrs(At, i, i < n, ac[r], av[r], ab[r], ae[r]);
+      ps[r] = T(0); as[r] = T(0);
+    }
+    lane_rows_dot<L, NR>(pc, pv, pb, pe, sl, xp, ps);
+    lane_rows_dot<L, NR>(ac, av, ab, ae, sl, xa, as);
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      const T p1 = subwarp_sum<L>(ps[r]), a1 = subwarp_sum<L>(as[r]);
+      const int i = base + r * step + sub;
+      if (i < n && sl == 0) fn(i, p1, a1);
+    }
   }
 }
 template <typename T, typename G, typename XP, typename XA, typename FN>

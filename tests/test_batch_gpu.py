@@ -148,3 +148,22 @@ def test_split_tail_matches_oracle(prec, cluster, tail, oracle_lib, monkeypatch)
         s1 = one.solution()
         assert s1["iter"][0] == sol["iter"][k]
         assert np.array_equal(s1["x"], xs[k])
+
+
+def test_autotune_picks_a_tile_and_restores_state(monkeypatch):
+    """The SpMV tile autotuner leaves every iterate as it found it: a solve after
+    tuning equals a solve of a fresh batch set up with the chosen tile."""
+    lib = load("f32")
+    probs = _mix(12, seed=11)
+    b = Batch(lib)
+    assert b.setup(probs, **WORKLOAD) == 0
+    tile = b.autotune(20)
+    assert tile in (4, 8, 16)
+    assert b.solve() == 0
+    s1 = b.solution()
+    monkeypatch.setenv("OSQP_GB300_LANE_TARGET", str(tile))
+    c = Batch(lib)
+    assert c.setup(probs, **WORKLOAD) == 0 and c.solve() == 0
+    s2 = c.solution()
+    assert np.array_equal(s1["iter"], s2["iter"])
+    assert np.array_equal(s1["x"], s2["x"])
