@@ -933,10 +933,12 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->kfn, b->threads, (size_t)b->dsm);
     b->grid = std::max(1, std::min(count, sms * std::max(per_sm, 1)));
   }
-  // Defaults measured on 4096 batched MPC QPs (GB300): one 1024-thread CTA
-  // per QP with staged vectors, and QPs still running after 1000 ADMM
-  // iterations continue on 8-CTA clusters with the QP in shared memory.
-  b->split = std::max(0, env_int("OSQP_GB300_BATCH_SPLIT", 1000));
+  // Defaults measured on 4096 batched MPC QPs (GB300, one box, alternating
+  // configurations): one 1024-thread CTA per QP with staged vectors (512 x 2
+  // per SM: -7 %), and QPs still running after 2000 ADMM iterations continue
+  // on 8-CTA clusters with the QP in shared memory (split 600: -10 %, 1000:
+  // -4 %; tail clusters of 16: -12 %, of 4: -1 %).
+  b->split = std::max(0, env_int("OSQP_GB300_BATCH_SPLIT", 2000));
   b->stage_mat = env_int("OSQP_GB300_BATCH_STAGE_MATRIX", 1) != 0;
   b->tail_cluster = std::max(0, std::min(16, env_int("OSQP_GB300_BATCH_TAIL", 8)));
   b->tail_grid = 0;
