@@ -600,6 +600,8 @@ struct OSQPBatch_ {
   int per_lane;           // SpMV tile: target entries per lane of a row's sub-warp
   std::vector<long long> nnzT_k, nnzA_k;   // per QP: entries of triu(P) and of A
   std::vector<int> order_h;                 // host copy of the queue order
+  std::vector<long long> work_h;            // per QP: entries + rows (cost of one pass)
+  int reorder;            // order the queue by the last solve's measured work
   float last_ms, last_step_ms;
   long long last_admm, last_pcg;
   std::vector<BatchInst> inst;
@@ -848,6 +850,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   BT_TRY(cudaMemcpyAsync(b->d_inst, b->inst.data(), sizeof(BatchInst) * count, cudaMemcpyHostToDevice, s));
   BT_TRY(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
   b->order_h = order;
+  b->work_h.assign(work.begin(), work.end());
   BT_TRY(cudaMemcpyAsync(B.Praw, Px, sizeof(T) * pto, cudaMemcpyDefault, s));
   BT_TRY(cudaMemcpyAsync(B.Araw, Ax, sizeof(T) * ao, cudaMemcpyDefault, s));
   BT_TRY(cudaMemcpyAsync(B.vn[1], q, sizeof(T) * nsum, cudaMemcpyDefault, s));
@@ -940,6 +943,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   // -4 %; tail clusters of 16: -12 %, of 4: -1 %).
   b->split = std::max(0, env_int("OSQP_GB300_BATCH_SPLIT", 2000));
   b->stage_mat = env_int("OSQP_GB300_BATCH_STAGE_MATRIX", 1) != 0;
+  b->reorder = env_int("OSQP_GB300_BATCH_REORDER", 1) != 0;
   b->tail_cluster = std::max(0, std::min(16, env_int("OSQP_GB300_BATCH_TAIL", 8)));
   b->tail_grid = 0;
   while (b->split > 0 && b->tail_cluster >= 1) {
@@ -1000,6 +1004,22 @@ extern "C" OSQPInt osqp_gb300_batch_solve(OSQPBatch* b) {
   else b->last_step_ms = b->last_ms;
   b->upd_pending = 0;
   b->last_admm = tot[0]; b->last_pcg = tot[1];
+  if (b->reorder && b->count > 1) {
+    // history-based queue order: the QPs that just took longest (PCG
+    // iterations x cost of one pass) go first next time, so the launch does
+    // not end with a few long QPs running on an otherwise idle GPU.  The
+    // order never changes a QP's result.
+    std::vector<BatchInfo> info(b->count);
+    BT_TRY(cudaMemcpy(info.data(), b->d_info, sizeof(BatchInfo) * b->count, cudaMemcpyDeviceToHost));
+    std::vector<int> order(b->count);
+    std::iota(order.begin(), order.end(), 0);
+    std::vector<double> key(b->count);
+    for (int k = 0; k < b->count; k++) key[k] = (double)(info[k].pcg + info[k].iter + 1) * (double)b->work_h[k];
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return key[a] > key[c]; });
+    BT_TRY(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * b->count, cudaMemcpyHostToDevice, b->stream));
+    BT_TRY(cudaStreamSynchronize(b->stream));
+    b->order_h = order;
+  }
   return 0;
 }
 
