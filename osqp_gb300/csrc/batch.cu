@@ -67,6 +67,7 @@ struct BatchInst {
   int n, m, n_off, m_off;
   int pt_off, a_off;    // offsets of the QP's triu-P and A entries (input order)
   int kktL, PL, AL, AtL;
+  int Pdiag_only;       // P holds exactly its full diagonal
 };
 
 template <typename TT>
@@ -86,6 +87,7 @@ struct BatchArrays {
     DevProblem<TT> pr;
     pr.n = b.n; pr.m = b.m;
     pr.P = CSR<TT>{Prow + b.n_off, Pcol, Pval, b.n, b.n, b.PL};
+    pr.P.diag = b.Pdiag_only;
     pr.A = CSR<TT>{Arow + b.m_off, Acol, Aval, b.m, b.n, b.AL};
     pr.At = CSR<TT>{Atrow + b.n_off, Atcol, Atval, b.n, b.m, b.AtL};
     pr.Pdiag = Pdiag + b.n_off; pr.Psrc = Psrc; pr.Asrc = Asrc;
@@ -773,15 +775,19 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   if (pto && cudaMemcpy(hPi.data(), Pi, sizeof(OSQPInt) * pto, cudaMemcpyDefault) != cudaSuccess) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
   long long ndiag = 0;
   for (int k = 0; k < count; k++) {
-    const BatchInst& I = b->inst[k];
+    BatchInst& I = b->inst[k];
     const OSQPInt* P = hPp.data() + pp_off[k];
+    int only_diag = 1;
     for (int j = 0; j < I.n; j++) {
       for (int e = P[j]; e < P[j + 1]; e++) {
         const OSQPInt r = hPi[I.pt_off + e];
         if (r > j) { delete b; return OSQP_DATA_VALIDATION_ERROR; }   // P must be upper triangular
-        if (r == j) { ndiag++; break; }
+        if (r != j) only_diag = 0;
       }
+      for (int e = P[j]; e < P[j + 1]; e++)
+        if (hPi[I.pt_off + e] == j) { ndiag++; break; }
     }
+    I.Pdiag_only = only_diag;
   }
   b->nnzPf = 2 * pto - 2 * ndiag + nsum;
   b->nnzT_k.resize(count); b->nnzA_k.resize(count);

@@ -526,6 +526,9 @@ struct CSR {
   const int* scol = nullptr;
   T* sval = nullptr;
   int srow = 0;
+  // every row holds exactly one entry, on the diagonal (a diagonal P): the
+  // product is one multiply per row, no sparse dot
+  int diag = 0;
 };
 
 

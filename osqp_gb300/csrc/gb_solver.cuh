@@ -133,7 +133,15 @@ __device__ __forceinline__ void kkt_rows_L(G& g, const CSR<T>& P, const CSR<T>& 
       row_ptrs(At, i, i < n, ac[r], av[r], ab[r], ae[r]);
       ps[r] = T(0); as[r] = T(0);
     }
-    lane_rows_dot<L, NR>(pc, pv, pb, pe, sl, xp, ps);
+    if (P.diag) {
+      // diagonal P: the row's one entry times x_i on the row's first lane
+      // (the sub-warp sum below adds zeros, so the value is the same)
+#pragma unroll
+      for (int r = 0; r < NR; r++)
+        if (sl == 0 && pb[r] < pe[r]) ps[r] = pv[r][pb[r]] * xp(base + r * step + sub);
+    } else {
+      lane_rows_dot<L, NR>(pc, pv, pb, pe, sl, xp, ps);
+    }
     lane_rows_dot<L, NR>(ac, av, ab, ae, sl, xa, as);
 #pragma unroll
     for (int r = 0; r < NR; r++) {
