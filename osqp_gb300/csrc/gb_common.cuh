@@ -112,6 +112,15 @@ template <> struct Acc<double> {
   __device__ __forceinline__ double value() const { return v; }
 };
 
+// a / b for double-float a = (ah, al), b = (bh, bl), rounded to float: one
+// correction step of the float quotient (Dekker's method; the remainder
+// ah - q bh is exact with an FMA), on the FP32 pipe.
+__device__ __forceinline__ float df_div(float ah, float al, float bh, float bl) {
+  const float q1 = __fdiv_rn(ah, bh);
+  const float r = __fmaf_rn(-q1, bh, ah) + (al - q1 * bl);
+  return q1 + __fdiv_rn(r, bh);
+}
+
 template <typename T>
 __device__ __forceinline__ T tmaxT(T a, T b) { return a > b ? a : (b == b ? b : a); }
 
@@ -157,6 +166,8 @@ struct GroupShared {
   double bdT[4];   // values of the iterate type (FP64 build)
   float bf[4];     // values of the iterate type (FP32 build)
   int bi[4];
+  // one-barrier CTA reductions (reduce1): per-warp (hi, lo, max), double-buffered
+  float r1[2][32][3];
 };
 
 // Broadcast slots of the iterate type T.
@@ -266,6 +277,28 @@ struct BlockGroup {
   template <typename T> __device__ void put(T* v, int i, T val) const { v[i] = val; }
   __device__ bool sync() { __syncthreads(); return true; }
   __device__ bool ok() const { return true; }
+
+  // One sum (double-float) and one maximum of the FP32 build across the CTA
+  // with a single barrier: every warp finishes the reduction itself from the
+  // per-warp partials (lane k reads warp k's; the same shuffle order in every
+  // warp, so every thread obtains the same bits).  The partials are
+  // double-buffered by `par` (flipped per call by every thread): a warp
+  // writing the next reduction's partials cannot overwrite ones a slower warp
+  // is still reading.
+  __device__ void reduce1(Acc<float>& s, float& m, int& par) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    warp_accT(s);
+    m = warp_maxT(m);
+    if (lane == 0) { sh->r1[par][w][0] = s.hi; sh->r1[par][w][1] = s.lo; sh->r1[par][w][2] = m; }
+    __syncthreads();
+    Acc<float> a;
+    float mm = 0.f;
+    if (lane < nw) { a.hi = sh->r1[par][lane][0]; a.lo = sh->r1[par][lane][1]; mm = sh->r1[par][lane][2]; }
+    warp_accT(a);
+    s = a;
+    m = warp_maxT(mm);
+    par ^= 1;
+  }
 
   // Reduce NS sums and NM maxima across the CTA; every thread receives the
   // FP64 results in rs / rm.  fn(rsum, rmax), if given, runs once (thread 0)

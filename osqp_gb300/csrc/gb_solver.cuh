@@ -463,6 +463,92 @@ struct Solver {
 
 
   // ---------------------------------------------------------------------
+  // The PCG of pcg_core for the FP32 build on one CTA with one barrier per
+  // reduction: every thread finishes each reduction (BlockGroup::reduce1) and
+  // keeps rTy as a double-float pair; alpha = rTy / pKp and beta =
+  // rTy_new / rTy are double-float quotients rounded to float (df_div), all on
+  // the FP32 pipe.  The stopping test ||r|| > eps is exact: ||r|| is a float
+  // and thr is the smallest float above eps.  Same recurrence and phases as
+  // pcg_core; barriers per iteration: 4 instead of 6.
+  // ---------------------------------------------------------------------
+  __device__ int pcg_core_block32(BlockGroup& g, double eps, float sig, float rho_s) {
+    const DevProblem<float> pr = this->pr;
+    const DevSettings s = this->s;
+    SolverScalars* const sc = this->sc;
+    const int n = pr.n, m = pr.m;
+    const bool vec = s.rho_is_vec && pr.rho_vec;
+    const int cg_max = s.cg_max_iter;
+    float* __restrict__ xp = pr.xp;
+    float thr = (float)eps;                        // smallest float > eps
+    if ((double)thr <= eps) thr = nextafterf(thr, INFINITY);
+    int par = 0;
+    // Phase I: r = K xp - rhs, yv = M^-1 r, p = -yv, rTy, ||r||
+    float* p = sc->p_parity ? pr.p1 : pr.p0;
+    Acc<float> rty;
+    float rn = 0.f;
+    kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return xp[c]; }, [&](int c) { return m ? pr.t[c] : 0.f; },
+      [&](int i, float pv, float av) {
+        const float kx = sig * xp[i] + pv + av;
+        const float r = kx - pr.rhs[i];
+        const float yv = pr.Minv[i] * r;
+        pr.r[i] = r; pr.yv[i] = yv; p[i] = -yv;
+        rty.add_prod(yv, r);
+        rn = tmax(rn, fabsf(r));
+      });
+    g.reduce1(rty, rn, par);
+    int it = 0;
+    bool cont = rn >= thr && 0 < cg_max;
+    while (cont) {
+      // Phase A: t = rho .* (A p)
+      if (m > 0) {
+        rows_rng(g, span_m(g, m), pr.A, [&](int c) { return p[c]; },
+                 [&](int j, float v) { pr.t[j] = (vec ? pr.rho_vec[j] : rho_s) * v; });
+        __syncthreads();
+      }
+      // Phase B: Kp = sigma p + P p + A' t ; pKp
+      Acc<float> pkp;
+      float dummy = 0.f;
+      kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return p[c]; }, [&](int c) { return m ? pr.t[c] : 0.f; },
+        [&](int i, float pv, float av) {
+          const float pi = p[i];
+          const float kp = sig * pi + pv + av;
+          pr.Kp[i] = kp;
+          pkp.add_prod(pi, kp);
+        });
+      g.reduce1(pkp, dummy, par);
+      const float at = df_div(rty.hi, rty.lo, pkp.hi, pkp.lo);
+      // Phase C: x += alpha p ; r += alpha Kp ; yv = M^-1 r ; rTy ; ||r||
+      Acc<float> rty_new;
+      float rn2 = 0.f;
+      for_n(g, n, [&](int i) {
+        xp[i] = xp[i] + at * p[i];
+        const float r = pr.r[i] + at * pr.Kp[i];
+        pr.r[i] = r;
+        const float yv = pr.Minv[i] * r;
+        pr.yv[i] = yv;
+        rty_new.add_prod(yv, r);
+        rn2 = tmax(rn2, fabsf(r));
+      });
+      g.reduce1(rty_new, rn2, par);
+      const float bt = df_div(rty_new.hi, rty_new.lo, rty.hi, rty.lo);
+      rty = rty_new;
+      it++;
+      cont = rn2 >= thr && it < cg_max;
+      // Phase D: p = beta p - yv (skipped when the loop is about to end)
+      if (cont) {
+        for_n(g, n, [&](int i) { p[i] = bt * p[i] - pr.yv[i]; });
+        __syncthreads();
+      }
+    }
+    if (threadIdx.x == 0) {
+      sc->pcg_iters_total += it;
+      if (it == 0) sc->zero_pcg_iters++; else sc->zero_pcg_iters = 0;
+    }
+    __syncthreads();
+    return it;
+  }
+
+  // ---------------------------------------------------------------------
   // PCG on the reduced KKT system K = P + sigma I + A' R A from the current
   // iterate xp and right-hand side rhs (cuda_pcg.cu:113-208): start-up
   // product r = K xp - rhs, then four phases per iteration.  t holds
@@ -470,6 +556,8 @@ struct Solver {
   // ---------------------------------------------------------------------
   template <typename G>
   __device__ int pcg_core(G& g, double eps, T sig, T rho_s) {
+    if constexpr (std::is_same<T, float>::value && std::is_same<G, BlockGroup>::value)
+      return pcg_core_block32(g, eps, sig, rho_s);
     // local copies: hot loops keep the pointers in registers instead of
     // re-reading them through `this` after every store
     const DevProblem<T> pr = this->pr;
