@@ -77,6 +77,11 @@ OSQPInt osqp_gb300_batch_stats(OSQPBatch* batch, double* kernel_ms, long long* a
  * to the end of the following solve (equals the solve time without an update). */
 OSQPInt osqp_gb300_batch_step_ms(OSQPBatch* batch, double* step_ms);
 
+/* Device time of every QP's last solve in seconds, from its first ADMM
+ * iteration to its last (count entries, host memory; a QP that moved to the
+ * tail form counts the time in between). */
+OSQPInt osqp_gb300_batch_qp_seconds(OSQPBatch* batch, double* seconds);
+
 /* PCG iterations of every QP in the last batch solve (count entries, host memory). */
 OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* batch, long long* pcg_iter);
 

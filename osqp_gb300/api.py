@@ -413,6 +413,13 @@ class Batch:
         return int(self.L.lib.osqp_gb300_batch_get_solution(self._h, cast(x_ptr), cast(y_ptr), None, None,
                                                             None, None, None))
 
+    def qp_seconds(self):
+        """Device time of every QP's last solve (seconds)."""
+        out = np.zeros(self.count, np.float64)
+        self.L.lib.osqp_gb300_batch_qp_seconds.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        self.L.lib.osqp_gb300_batch_qp_seconds(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
     def pcg_iters(self):
         out = np.zeros(self.count, np.int64)
         self.L.lib.osqp_gb300_batch_pcg_iters(self._h, out.ctypes.data_as(C.POINTER(C.c_longlong)))

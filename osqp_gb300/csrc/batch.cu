@@ -483,7 +483,7 @@ __global__ void k_batch_check_bounds(const TT* l, const TT* u, long long msum, i
     if (l[j] > u[j]) atomicExch(bad, 1);
 }
 
-struct BatchInfo { int status, iter; long long pcg; double obj, prim, dual; };
+struct BatchInfo { int status, iter; long long pcg; double obj, prim, dual, seconds; };
 
 __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out, long long* totals) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
@@ -493,6 +493,7 @@ __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out,
     out[k].obj = st[k].obj_val;
     out[k].prim = st[k].prim_res;
     out[k].dual = st[k].dual_res;
+    out[k].seconds = st[k].elapsed;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     long long a = 0, p = 0;
@@ -1124,6 +1125,14 @@ extern "C" OSQPInt osqp_gb300_batch_get_solution(OSQPBatch* b, OSQPFloat* x, OSQ
 extern "C" OSQPInt osqp_gb300_batch_step_ms(OSQPBatch* b, double* step_ms) {
   if (!b || !step_ms) return OSQP_WORKSPACE_NOT_INIT_ERROR;
   *step_ms = b->last_step_ms;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_qp_seconds(OSQPBatch* b, double* seconds) {
+  if (!b || !seconds) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  std::vector<BatchInfo> info(b->count);
+  BT_TRY(cudaMemcpy(info.data(), b->d_info, sizeof(BatchInfo) * b->count, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < b->count; k++) seconds[k] = info[k].seconds;
   return 0;
 }
 
