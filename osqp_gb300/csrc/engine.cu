@@ -7,7 +7,9 @@
 //   osqp_update_*        osqp_api.c:1184-1530
 //   osqp_warm_start      osqp_api.c:1260-1304
 // The ADMM loop itself runs on the device (gb_solver.cuh) in one launch:
-// a single CTA for small problems, a cooperative persistent grid otherwise.
+// a single CTA for small problems, one thread-block cluster (16 CTAs, else
+// 8, else one CTA) for medium ones, a cooperative persistent grid for large
+// ones (OSQP_GB300_MODE = block | grid | clusterN overrides the choice).
 // Every CUDA failure is returned as an OSQP error code; nothing calls exit().
 #include <cuda_runtime.h>
 #include <math.h>

@@ -1,14 +1,17 @@
 // gb_common.cuh -- shared device building blocks of the GB300 OSQP engine.
 //
-// * Group abstraction: the same device code runs an OSQP solve either on one
-//   CTA (BlockGroup: batched instances, small problems; barrier =
-//   __syncthreads) or on a cooperative persistent grid (GridGroup: one large
-//   QP; barrier = bounded generation-counter grid barrier).
-// * Deterministic reductions: every reduction is summed in FP64 in a fixed
-//   order (warp shuffle tree, warps in index order, blocks in index order), so
-//   a rerun reproduces every bit and all CTAs of a grid obtain identical
+// * Group abstraction: the same device code runs an OSQP solve on one CTA
+//   (BlockGroup: batched instances, small problems; barrier = __syncthreads),
+//   on a thread-block cluster (ClusterGroup: contiguous row slices per CTA,
+//   hardware cluster barrier, partials exchanged through distributed shared
+//   memory) or on a cooperative persistent grid (GridGroup: one large QP;
+//   barrier = bounded generation-counter grid barrier).
+// * Deterministic reductions: sums are accumulated in double-float (FP32
+//   build) or FP64 and combined in a fixed order (lanes, warps, CTAs, ranks),
+//   so a rerun reproduces every bit and all CTAs of a group obtain identical
 //   scalars, which lets each CTA keep its own copy of the solver's scalar state.
-// * CSR row kernels with 1..32 lanes per row (sub-warp per row).
+// * CSR row kernels with 1..32 lanes per row (sub-warp per row), several rows
+//   in flight per lane group.
 #pragma once
 
 #include <cooperative_groups.h>
