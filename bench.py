@@ -80,10 +80,10 @@ def make_workload(count, steps, seed=3):
 
 # DRAM bytes per algorithmic byte of the CTA-form solve launch, from the ncu
 # capture of 304 batched MPC QPs (profiles/k_batch_solve_mpc304.md:
-# 67.3 + 8.3 GB DRAM for 285.6 GB algorithmic).  The 4096-QP launch is too
+# 52.2 + 7.0 GB DRAM for 285.6 GB algorithmic).  The 4096-QP launch is too
 # long to capture under the size rule; its traffic is this ratio times its
 # algorithmic bytes (the matrices of the QPs in flight stay L2-resident in both).
-TRAFFIC_PER_ALGORITHMIC_BYTE = (67.304107 + 8.307210) / 285.586664900
+TRAFFIC_PER_ALGORITHMIC_BYTE = (52.202385 + 6.987452) / 285.586664900
 
 
 def measured_peak():
@@ -244,7 +244,7 @@ def gpu_arm(args, probs, ls, us):
     b = Batch(lib)
     rc = b.setup(probs, **settings)
     assert rc == 0, f"batch setup failed: {rc}"
-    tile = b.autotune(30)      # SpMV tile (entries per lane), timed on a sample; state restored
+    tile = b.autotune(60)      # SpMV tile (entries per lane), timed on a sample; state restored
     count = b.count
     K, W = args.steps, args.warmup
     nsteps = K + W

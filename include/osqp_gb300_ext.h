@@ -61,9 +61,10 @@ OSQPInt osqp_gb300_batch_get_solution(OSQPBatch* batch, OSQPFloat* x, OSQPFloat*
                                       OSQPFloat* dual_res);
 
 /* SpMV tile autotuner: times a short solve (probe_iter ADMM iterations; <= 0
- * means 30) of a sample of the batch for several targets of matrix entries
- * per lane of a row's sub-warp, keeps the fastest for every later solve and
- * returns it in *per_lane (may be NULL).  Every iterate and scalar of the
+ * means 60) of a sample of the batch for several targets of matrix entries
+ * per lane of a row's sub-warp (8, 4, 16), keeps the fastest for every later
+ * solve (the default 8 unless another is more than 3 % faster) and returns it
+ * in *per_lane (may be NULL).  Every iterate and scalar of the
  * batch is restored afterwards.  The tile changes the summation order inside
  * a row, so results are reproducible for a given tile; the default tile
  * (OSQP_GB300_LANE_TARGET, 8) does not depend on the batch. */

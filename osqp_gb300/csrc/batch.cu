@@ -1038,7 +1038,7 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
   if (!b) return OSQP_WORKSPACE_NOT_INIT_ERROR;
   cudaSetDevice(b->device);
   cudaStream_t s = b->stream;
-  const int probe = std::max(1, std::min((int)(probe_iter > 0 ? probe_iter : 30), b->ds.max_iter));
+  const int probe = std::max(1, std::min((int)(probe_iter > 0 ? probe_iter : 60), b->ds.max_iter));
   const int ns = std::max(1, std::min(b->count, b->grid));   // one QP per resident CTA / cluster
   std::vector<int> sample(ns);
   for (int i = 0; i < ns; i++) sample[i] = b->order_h[(long long)i * b->count / ns];
@@ -1061,8 +1061,8 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
   if (!rc) cudaMemcpyAsync(snap + off, B.st, sbytes, cudaMemcpyDeviceToDevice, s);
   if (!rc) cudaMemcpyAsync(dbuf, sample.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s);
   LaunchBufs lb{dbuf, ns, dbuf + 2 * (size_t)ns, dbuf + ns};
-  float best_ms = 1e30f;
-  for (int cand : {4, 8, 16}) {
+  float best_ms = 1e30f, default_ms = 1e30f;
+  for (int cand : {kDefaultPerLane, 4, 16}) {
     if (rc) break;
     assign_lanes(b, cand);
     cudaMemcpyAsync(b->d_inst, b->inst.data(), sizeof(BatchInst) * b->count, cudaMemcpyHostToDevice, s);
@@ -1078,8 +1078,11 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
       cudaEventElapsedTime(&t, e0, e1);
       ms = std::min(ms, t);
     }
+    if (cand == kDefaultPerLane) default_ms = ms;
     if (ms < best_ms) { best_ms = ms; best = cand; }
   }
+  // keep the default tile unless another one is clearly faster on the probe
+  if (best != kDefaultPerLane && best_ms > 0.97f * default_ms) best = kDefaultPerLane;
   // the chosen tile, and every vector and scalar as before the probes
   assign_lanes(b, best);
   cudaMemcpyAsync(b->d_inst, b->inst.data(), sizeof(BatchInst) * b->count, cudaMemcpyHostToDevice, s);
