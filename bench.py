@@ -535,10 +535,10 @@ def main():
     ap.add_argument("--count", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--serve-rate", type=float, default=20.0, help="served form: Poisson arrivals (req/s); 0 = skip")
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="served form: Poisson arrivals (req/s); 0 = skip")
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--serve-streams", type=int, default=128, help="recurring problems per class")
-    ap.add_argument("--serve-concurrency", type=int, default=16, help="launches in flight")
+    ap.add_argument("--serve-concurrency", type=int, default=32, help="launches in flight")
     ap.add_argument("--config", default="mpc_batch", choices=["mpc_batch", "large_sparse", "svm"])
     ap.add_argument("--oracle-timeout", type=float, default=900.0,
                     help="single-QP configs: seconds allowed for the FP64 CPU oracle (0 = skip)")
