@@ -35,7 +35,8 @@ OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter, long long
  *   A: CSC, likewise Ap / Ai / Ax.
  *   q concatenated (sum n), l and u concatenated (sum m).
  * Pointers may be host or device memory.  Settings apply to every QP
- * (linsys_solver must be OSQP_INDIRECT_SOLVER). */
+ * (linsys_solver must be OSQP_INDIRECT_SOLVER).  A batch is used by one host
+ * thread at a time (the server below owns the pools it serves). */
 typedef struct OSQPBatch_ OSQPBatch;
 
 OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, const OSQPInt* n, const OSQPInt* m,
@@ -121,7 +122,8 @@ OSQPInt osqp_gb300_server_wait(OSQPServer* server, long long ticket, OSQPFloat* 
                                OSQPInt* iter, OSQPFloat* obj_val, double* latency_ms);
 
 /* Stop the worker after the queued requests complete and free the server
- * (the pools stay owned by the caller). */
+ * (the pools stay owned by the caller).  Call it after every ticket has been
+ * waited for; tickets not waited for are discarded. */
 OSQPInt osqp_gb300_server_destroy(OSQPServer* server);
 
 #ifdef __cplusplus

@@ -41,16 +41,6 @@ namespace gbp {
 constexpr int kPolishThreads = 1024;
 constexpr int kPolishCgMaxIter = 10000;
 
-#define PL_TRY(call)                                                              \
-  do {                                                                            \
-    cudaError_t _e = (call);                                                      \
-    if (_e != cudaSuccess) {                                                      \
-      fprintf(stderr, "osqp_gb300 polish: %s failed: %s (%s:%d)\n", #call,        \
-              cudaGetErrorString(_e), __FILE__, __LINE__);                        \
-      return -1;                                                                  \
-    }                                                                             \
-  } while (0)
-
 // Result of one polish launch (device -> host).
 struct PolishOut {
   int accepted;
@@ -280,7 +270,11 @@ int gb_polish_run(OSQPSolver* solver) {
   cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, (int*)nullptr, (int*)nullptr, std::max(n, m) + 1, s);
   const size_t o_tmp = pl.take(tmp_bytes);
   char* ws = nullptr;
-  PL_TRY(cudaMallocAsync((void**)&ws, pl.off, s));
+  if (cudaMallocAsync((void**)&ws, pl.off, s) != cudaSuccess) {
+    cudaGetLastError();
+    info->status_polish = OSQP_POLISH_FAILED;
+    return OSQP_MEM_ALLOC_ERROR;
+  }
   auto P_ = [&](size_t o) { return (void*)(ws + o); };
   int* flags = (int*)P_(o_flags); int* act = (int*)P_(o_act); int* red = (int*)P_(o_red);
   int* rl = (int*)P_(o_rl); int* aoff = (int*)P_(o_aoff); int* atc = (int*)P_(o_atc);
