@@ -164,11 +164,11 @@ struct Stager {
   // entries of rows [lo, hi); rowptr holds global positions.  When they do
   // not all fit, the entries of the longest prefix of rows that fits go on
   // chip (M.scol / M.sval for rows below M.srow) and the rest stay in HBM.
-  __device__ __forceinline__ void entries(CSR<TT>& M, const int* grow, int lo, int hi) {
+  __device__ __forceinline__ void entries(CSR<TT>& M, const int* grow, int lo, int hi, int share = 1) {
     if (hi <= lo) return;
     const int k0 = grow[lo], k1 = grow[hi];
     if (k1 <= k0) return;
-    const long long room = (long long)(cap - off) / 4 - 8;      // words, less alignment slack
+    const long long room = (long long)(cap - off) / 4 / share - 8;   // words, less alignment slack
     const long long fit = room > 0 ? room / (1 + W) : 0;         // entries
     int rs = hi;
     if ((long long)(k1 - k0) > fit) {                             // largest rs with grow[rs] - k0 <= fit
@@ -201,7 +201,8 @@ struct Stager {
 
 template <typename TT>
 __device__ __forceinline__ bool stage_problem(DevProblem<TT>& pr, const Spans& sp, bool rho_vec,
-                                              unsigned char* base, int cap, int dir, bool matrices = true) {
+                                              unsigned char* base, int cap, int dir, bool matrices = true,
+                                              bool matrices_first = false) {
   Stager<TT> sg{base, cap, 0, dir};
   const int n = pr.n, m = pr.m;
   const int nlo = sp.nlo, nhi = n < sp.nhi ? n : sp.nhi;
@@ -219,16 +220,21 @@ __device__ __forceinline__ bool stage_problem(DevProblem<TT>& pr, const Spans& s
   if (m) q.A.rowptr = sg.rows(pr.A.rowptr, mlo, mhi);
   q.At.rowptr = sg.rows(pr.At.rowptr, nlo, nhi);
   q.P.rowptr = sg.rows(pr.P.rowptr, nlo, nhi);
-  q.Minv = sg.span(pr.Minv, nlo, nhi, true);
-  q.r = sg.span(pr.r, nlo, nhi, false);
-  q.yv = sg.span(pr.yv, nlo, nhi, false);
-  q.Kp = sg.span(pr.Kp, nlo, nhi, false);
-  q.rhs = sg.span(pr.rhs, nlo, nhi, false);
+  auto streamed = [&]() {
+    q.Minv = sg.span(pr.Minv, nlo, nhi, true);
+    q.r = sg.span(pr.r, nlo, nhi, false);
+    q.yv = sg.span(pr.yv, nlo, nhi, false);
+    q.Kp = sg.span(pr.Kp, nlo, nhi, false);
+    q.rhs = sg.span(pr.rhs, nlo, nhi, false);
+  };
+  if (!matrices_first) streamed();
   if (matrices) {
-    if (m) sg.entries(q.A, growA, mlo, mhi);
+    // matrices first: A may take half of the room, A' the rest of it
+    if (m) sg.entries(q.A, growA, mlo, mhi, matrices_first ? 2 : 1);
     sg.entries(q.At, growAt, nlo, nhi);
     sg.entries(q.P, growP, nlo, nhi);
   }
+  if (matrices_first) streamed();
   pr = q;
   return true;
 }
@@ -272,7 +278,7 @@ __device__ Spans cluster_spans(const DevProblem<TT>& pr, int kktL, int r, int c)
 template <typename TT, typename G>
 __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s, int k, int mode,
                            GroupShared& gsh, SolverScalars& ssc, unsigned char* dsm, int dsm_bytes,
-                           int it_lo, int it_hi, bool stage_mat) {
+                           int it_lo, int it_hi, int stage_mat) {
   DevProblem<TT> pv = B.problem(k);
   if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pv.st; }
   __syncthreads();
@@ -282,7 +288,7 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
       g.sp = cluster_spans(pv, B.inst[k].kktL, (int)g.rank, (int)g.size);
       g.sliced = true;
     }
-    staged = stage_problem(pv, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, 1, stage_mat);
+    staged = stage_problem(pv, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, 1, stage_mat != 0, stage_mat == 2);
     if constexpr (std::is_same<G, ClusterGroup>::value) g.repl = staged;
     g.sync();   // staged copies complete in every CTA before any peer writes them
   }
@@ -312,7 +318,7 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   g.sync();
   if (staged) {
     DevProblem<TT> pb = B.problem(k);
-    stage_problem(pb, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, -1, stage_mat);
+    stage_problem(pb, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, -1, stage_mat != 0, stage_mat == 2);
     g.sync();   // peers may still read this CTA's copies until here
   }
   if constexpr (std::is_same<G, ClusterGroup>::value) {
@@ -355,7 +361,7 @@ k_batch(BatchArrays<TT> B, DevSettings s, BatchLaunch L) {
     __syncthreads();
     if (idx >= count) break;
     batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi,
-               L.stage_mat != 0);
+               L.stage_mat);
     if (threadIdx.x == 0) *B.problem(L.order[idx]).st = ssc;
     __syncthreads();
   }
@@ -379,7 +385,7 @@ k_batch_cluster(BatchArrays<TT> B, DevSettings s, BatchLaunch L) {
     cl.sync();   // rank 0 keeps its shared memory until every CTA has read idx
     if (idx >= count) break;
     batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi,
-               L.stage_mat != 0);
+               L.stage_mat);
     if (g.rank == 0 && threadIdx.x == 0) *B.problem(L.order[idx]).st = ssc;
     cl.sync();
   }
@@ -949,7 +955,9 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   // on 8-CTA clusters with the QP in shared memory (split 600: -10 %, 1000:
   // -4 %; tail clusters of 16: -12 %, of 4: -1 %).
   b->split = std::max(0, env_int("OSQP_GB300_BATCH_SPLIT", 2000));
-  b->stage_mat = env_int("OSQP_GB300_BATCH_STAGE_MATRIX", 1) != 0;
+  // 0: vectors only; 1: vectors, then matrix rows; 2: matrix rows before the
+  // element-wise PCG vectors
+  b->stage_mat = std::max(0, std::min(2, env_int("OSQP_GB300_BATCH_STAGE_MATRIX", 1)));
   b->reorder = env_int("OSQP_GB300_BATCH_REORDER", 1) != 0;
   b->tail_cluster = std::max(0, std::min(16, env_int("OSQP_GB300_BATCH_TAIL", 8)));
   b->tail_grid = 0;
