@@ -53,6 +53,7 @@ sys.path.insert(0, REPO)
 
 from osqp_gb300 import problems as pb  # noqa: E402
 from osqp_gb300.roofline import solve_bytes, pfull_nnz  # noqa: E402
+from osqp_gb300.api import BLOCK_DIAGONAL_PRECONDITIONER  # noqa: E402
 
 SETTINGS = dict(rho=0.1, sigma=1e-6, alpha=1.6, scaling=10, eps_abs=1e-3, eps_rel=1e-3, rho_is_vec=1,
                 check_termination=5, adaptive_rho_tolerance=5.0, max_iter=4000, check_dualgap=1,
@@ -289,7 +290,8 @@ def gpu_arm(args, probs, ls, us):
         admm_tot += int(sol["iter"].sum()); pcg_tot += int(pcg.sum())
         for k, (P, q, A, l, u) in enumerate(probs):
             bytes_alg += solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, 4, int(sol["iter"][k]),
-                                     int(pcg[k]), SETTINGS["check_termination"])
+                                     int(pcg[k]), SETTINGS["check_termination"],
+                                     SETTINGS.get("cg_precond", 1) == BLOCK_DIAGONAL_PRECONDITIONER)
     torch.cuda.synchronize(); barrier()
     clk = clocks.stop()
     status_last = sol["status"].copy()
@@ -406,7 +408,8 @@ def single_config(args):
         stt = solver.stats()
         obj, prim, dual = _host_residuals(data, r.x, r.y)
         kms = stt["kernel_ms"]
-        byt = solve_bytes(n, m, nnz_pf, A.nnz, w, stt["admm_iter"], stt["pcg_iter"], st["check_termination"])
+        byt = solve_bytes(n, m, nnz_pf, A.nnz, w, stt["admm_iter"], stt["pcg_iter"], st["check_termination"],
+                          st.get("cg_precond", 1) == BLOCK_DIAGONAL_PRECONDITIONER)
         out["paths"][prec] = {
             "status": r.info["status"], "status_polish": r.info["status_polish"], "admm_iter": stt["admm_iter"],
             "pcg_iter": stt["pcg_iter"], "solve_kernel_ms": kms, "solve_wall_ms": wall * 1e3,
@@ -544,8 +547,12 @@ def main():
                     help="single-QP configs: seconds allowed for the FP64 CPU oracle (0 = skip)")
     ap.add_argument("--max-iter", type=int, default=SETTINGS["max_iter"],
                     help="ADMM iteration cap (smaller values give short profiling cases)")
+    ap.add_argument("--precond", default="diagonal", choices=["diagonal", "block"],
+                    help="PCG preconditioner: OSQP's diagonal (Jacobi) one or the 32 x 32 block-Jacobi one")
     args = ap.parse_args()
     SETTINGS["max_iter"] = args.max_iter
+    if args.precond == "block":
+        SETTINGS["cg_precond"] = BLOCK_DIAGONAL_PRECONDITIONER
     if args.config != "mpc_batch":
         single_config(args)
         return
@@ -555,7 +562,8 @@ def main():
     config = {"workload": f"mpc_batch: {args.count} linear-MPC QPs (T~U{{10..50}}, nx~U{{8..40}}, nu~U{{4..16}}), "
                           "new x0 per step, cold solve to eps 1e-3",
               "qps_per_step": args.count, "eps": 1e-3, "settings": "rho_is_vec=1, check_termination=5, "
-              "adaptive_rho, scaling=10, check_dualgap=1", "l2": "inputs (~3 GB of CSR data) exceed the 129 MB L2",
+              "adaptive_rho, scaling=10, check_dualgap=1",
+              "preconditioner": "block-Jacobi 32x32" if args.precond == "block" else "diagonal (Jacobi)", "l2": "inputs (~3 GB of CSR data) exceed the 129 MB L2",
               "parallelism": f"replicas x{world}"}
     metric = "QP solves/s (batched MPC, eps 1e-3)"
 

@@ -3,7 +3,8 @@
  *
  * These have no counterpart in the reference's public API; they expose what
  * the device engine measures or adds (statistics of the last solve, the
- * batched many-QP solver, the request-serving loop).
+ * block-Jacobi preconditioner, the batched many-QP solver, the
+ * request-serving loop).
  */
 #ifndef OSQP_GB300_EXT_H
 #define OSQP_GB300_EXT_H
@@ -20,6 +21,23 @@ extern "C" {
  * Returns 0 on success. */
 OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter, long long* pcg_iter,
                                double* kernel_ms, OSQPInt* grid_form);
+
+/* ---- Block-Jacobi preconditioner -------------------------------------------
+ * settings->cg_precond = OSQP_GB300_BLOCK_DIAGONAL_PRECONDITIONER (an
+ * extension of osqp_precond_type, include/public/osqp_api_constants.h:66-69,
+ * which has the none and diagonal values only) preconditions the reduced-KKT
+ * PCG with the inverted 32 x 32 diagonal blocks of K = P + sigma I + A' R A
+ * (variables [32 b, 32 b + 32)), rebuilt on the device whenever rho changes.
+ * Accepted by osqp_setup, osqp_update_settings, the batched solver and the
+ * algebra library's linear-system solver.  The polish keeps the diagonal
+ * preconditioner. */
+#define OSQP_GB300_BLOCK_DIAGONAL_PRECONDITIONER 2
+
+/* Copies the current block-Jacobi blocks of M^-1 (scaled problem) into `out`
+ * (host or device memory; ceil(n / 32) * 1024 values, block b at 1024 b,
+ * entry (j, i) at 32 j + i, zeros past n) and returns the number of values; `out` NULL
+ * returns the count only.  Returns 0 when the solver has no blocks. */
+OSQPInt osqp_gb300_precond_blocks(OSQPSolver* solver, OSQPFloat* out);
 
 /* ---- Batched solver --------------------------------------------------------
  * Many independent QPs of uneven size solved in one persistent launch: a CTA

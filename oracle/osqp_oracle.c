@@ -287,6 +287,7 @@ typedef struct {
   /* indirect: reduced-KKT PCG (cuda_pcg.cu:50-285, cuda_pcg_interface.cu:32-361) */
   const ocsc* P; const ocsc* A; const double* rho_vec; double rho;
   double *x, *p, *Kp, *yv, *r, *rhs, *zt, *Pdiag, *precond_inv;
+  double *binv, *bwork_m;   /* block-Jacobi (cg_precond = 2): 32 x 32 blocks, dense scatter of A columns */
   OSQPInt max_iter, reduction_threshold, zero_pcg_iters, precond_type;
   double tol_fraction, reduction_factor, eps_prev;
   const double *scaled_prim_res, *scaled_dual_res;
@@ -460,9 +461,100 @@ static void pcg_matvec(oc_ls* s, const double* x, double* y) {
   pcg_rho_apply(s, s->zt);
   csc_atxpy(s->A, s->zt, y, 1.0, 1.0);
 }
+/* Block-Jacobi preconditioner of the GB300 solver (cg_precond = 2; the
+ * reference's PCG has the diagonal one only).  Blocks are the variables
+ * [32 b, 32 b + 32); block b of M^-1 = inverse of the block of
+ * K = P + sigma I + A' R A, stored densely at binv + 1024 b (row-major, the
+ * block is symmetric).  Inverted through a Cholesky factorisation; a block
+ * with a non-positive pivot keeps 1 / K_ii on its diagonal. */
+#define OC_PBLK 32
+static void pcg_block_precond(oc_ls* s) {
+  OSQPInt n = s->n, b, nblk = (n + OC_PBLK - 1) / OC_PBLK;
+  double K[OC_PBLK][OC_PBLK], L[OC_PBLK][OC_PBLK], W[OC_PBLK][OC_PBLK];
+  for (b = 0; b < nblk; b++) {
+    OSQPInt i0 = b * OC_PBLK, nb = (n - i0 < OC_PBLK) ? n - i0 : OC_PBLK, a, c, k, e;
+    double* Bb = s->binv + (size_t)b * OC_PBLK * OC_PBLK;
+    int ok = 1;
+    memset(K, 0, sizeof(K));
+    /* P from its upper triangle */
+    for (c = 0; c < nb; c++)
+      for (k = s->P->p[i0 + c]; k < s->P->p[i0 + c + 1]; k++) {
+        OSQPInt r = s->P->i[k] - i0;
+        if (r < 0 || r >= nb) continue;
+        K[r][c] += s->P->x[k];
+        if (r != c) K[c][r] += s->P->x[k];
+      }
+    /* A' R A: column c of A scattered densely, dotted with columns a >= c */
+    for (c = 0; c < nb; c++) {
+      for (k = s->A->p[i0 + c]; k < s->A->p[i0 + c + 1]; k++) s->bwork_m[s->A->i[k]] = s->A->x[k];
+      for (a = c; a < nb; a++) {
+        double d = 0.0;
+        for (e = s->A->p[i0 + a]; e < s->A->p[i0 + a + 1]; e++) {
+          OSQPInt row = s->A->i[e];
+          double rr = s->rho_vec ? s->rho_vec[row] : s->rho;
+          d += rr * s->bwork_m[row] * s->A->x[e];
+        }
+        K[a][c] += d;
+        if (a != c) K[c][a] += d;
+      }
+      for (k = s->A->p[i0 + c]; k < s->A->p[i0 + c + 1]; k++) s->bwork_m[s->A->i[k]] = 0.0;
+    }
+    for (c = 0; c < nb; c++) K[c][c] += s->sigma;
+    /* K = L L' */
+    memset(L, 0, sizeof(L));
+    for (c = 0; c < nb && ok; c++) {
+      double d = K[c][c];
+      for (k = 0; k < c; k++) d -= L[c][k] * L[c][k];
+      if (!(d > 0.0) || !isfinite(d)) { ok = 0; break; }
+      L[c][c] = sqrt(d);
+      for (a = c + 1; a < nb; a++) {
+        double v = K[a][c];
+        for (k = 0; k < c; k++) v -= L[a][k] * L[c][k];
+        L[a][c] = v / L[c][c];
+      }
+    }
+    memset(Bb, 0, sizeof(double) * OC_PBLK * OC_PBLK);
+    if (!ok) {
+      for (c = 0; c < nb; c++) Bb[c * OC_PBLK + c] = 1.0 / K[c][c];
+      continue;
+    }
+    /* W = L^-1 (forward substitution on unit vectors), M^-1 = W' W */
+    memset(W, 0, sizeof(W));
+    for (c = 0; c < nb; c++)
+      for (a = c; a < nb; a++) {
+        double v = (a == c) ? 1.0 : 0.0;
+        for (k = c; k < a; k++) v -= L[a][k] * W[k][c];
+        W[a][c] = v / L[a][a];
+      }
+    for (a = 0; a < nb; a++)
+      for (c = 0; c < nb; c++) {
+        double v = 0.0;
+        for (k = (a > c ? a : c); k < nb; k++) v += W[k][a] * W[k][c];
+        Bb[a * OC_PBLK + c] = v;
+      }
+  }
+}
+static void pcg_block_apply(const oc_ls* s, const double* r, double* y) {
+  OSQPInt n = s->n, i, j;
+  for (i = 0; i < n; i++) {
+    OSQPInt b0 = i - i % OC_PBLK, nb = (n - b0 < OC_PBLK) ? n - b0 : OC_PBLK;
+    const double* row = s->binv + (size_t)b0 * OC_PBLK + (size_t)(i - b0) * OC_PBLK;
+    double v = 0.0;
+    for (j = 0; j < nb; j++) v += row[j] * r[b0 + j];
+    y[i] = v;
+  }
+}
+
 /* cuda_pcg.cu:211-285 */
 static void pcg_update_precond(oc_ls* s) {
   OSQPInt j, k;
+  if (s->precond_type == 2) {
+    if (!s->binv) {
+      s->binv = vnew(((s->n + OC_PBLK - 1) / OC_PBLK) * OC_PBLK * OC_PBLK);
+      s->bwork_m = vnew(s->m > 0 ? s->m : 1);
+    }
+    pcg_block_precond(s);
+  }
   if (s->precond_type == OSQP_NO_PRECONDITIONER) {
     for (j = 0; j < s->n; j++) s->precond_inv[j] = 1.0;
     return;
@@ -504,14 +596,17 @@ static OSQPInt pcg_run(oc_ls* s, double eps) {
   pcg_matvec(s, s->x, s->r);
   for (j = 0; j < n; j++) s->r[j] -= s->rhs[j];
   rnorm = vnorm_inf(s->r, n);
-  for (j = 0; j < n; j++) { s->yv[j] = s->precond_inv[j] * s->r[j]; s->p[j] = -s->yv[j]; }
+  if (s->precond_type == 2) pcg_block_apply(s, s->r, s->yv);
+  else for (j = 0; j < n; j++) s->yv[j] = s->precond_inv[j] * s->r[j];
+  for (j = 0; j < n; j++) s->p[j] = -s->yv[j];
   rTy = vdot(s->yv, s->r, n);
   while (rnorm > eps && it < s->max_iter) {
     pcg_matvec(s, s->p, s->Kp);
     pKp = vdot(s->p, s->Kp, n);
     alpha = rTy / pKp;
     for (j = 0; j < n; j++) { s->x[j] += alpha * s->p[j]; s->r[j] += alpha * s->Kp[j]; }
-    for (j = 0; j < n; j++) s->yv[j] = s->precond_inv[j] * s->r[j];
+    if (s->precond_type == 2) pcg_block_apply(s, s->r, s->yv);
+    else for (j = 0; j < n; j++) s->yv[j] = s->precond_inv[j] * s->r[j];
     rTy_prev = rTy;
     rTy = vdot(s->yv, s->r, n);
     rnorm = vnorm_inf(s->r, n);
@@ -566,6 +661,8 @@ static int ls_init(oc_ls** out, const ocsc* P, const ocsc* A, const double* rho_
     s->max_iter = st->cg_max_iter; s->reduction_threshold = st->cg_tol_reduction;
     s->tol_fraction = st->cg_tol_fraction; s->reduction_factor = st->cg_tol_fraction;
     s->precond_type = st->cg_precond;
+    /* the GB300 polish runs its PCG with the diagonal preconditioner */
+    if (polishing && s->precond_type == 2) s->precond_type = OSQP_DIAGONAL_PRECONDITIONER;
     s->scaled_prim_res = spr; s->scaled_dual_res = sdr;
     pcg_update_precond(s);
   }
@@ -613,7 +710,7 @@ static void ls_free(oc_ls* s) {
   free(s->Lp); free(s->Li); free(s->etree); free(s->Lnz); free(s->iwork); free(s->bwork);
   free(s->Lx); free(s->D); free(s->Dinv); free(s->fwork); free(s->bp); free(s->sol); free(s->rho_inv_vec);
   free(s->x); free(s->p); free(s->Kp); free(s->yv); free(s->r); free(s->rhs); free(s->zt);
-  free(s->Pdiag); free(s->precond_inv);
+  free(s->Pdiag); free(s->precond_inv); free(s->binv); free(s->bwork_m);
   free(s);
 }
 
@@ -1434,3 +1531,13 @@ OSQPInt osqp_update_settings(OSQPSolver* solver, const OSQPSettings* ns) {
 
 /* Total PCG iterations of the last solve (oracle diagnostics only). */
 OSQPInt oracle_last_pcg_iters(OSQPSolver* solver) { return solver && solver->work ? solver->work->pcg_iters_total : 0; }
+/* The block-Jacobi blocks (cg_precond = 2, indirect solver): copies
+ * ceil(n / 32) * 1024 values into out; returns how many, 0 when there are none. */
+OSQPInt oracle_block_inverse(OSQPSolver* solver, double* out) {
+  oc_ls* l;
+  size_t cnt;
+  if (!solver || !solver->work || !(l = solver->work->ls) || l->type != OSQP_INDIRECT_SOLVER || !l->binv) return 0;
+  cnt = (size_t)((l->n + OC_PBLK - 1) / OC_PBLK) * OC_PBLK * OC_PBLK;
+  if (out) memcpy(out, l->binv, sizeof(double) * cnt);
+  return (OSQPInt)cnt;
+}

@@ -34,6 +34,10 @@ UNSOLVED = 11
 
 DIRECT_SOLVER = 1
 INDIRECT_SOLVER = 2
+# cg_precond values: OSQP's none / diagonal, and the GB300 block-Jacobi option
+NO_PRECONDITIONER = 0
+DIAGONAL_PRECONDITIONER = 1
+BLOCK_DIAGONAL_PRECONDITIONER = 2
 
 STATUS_NAMES = {
     1: "solved", 2: "solved inaccurate", 3: "primal infeasible",
@@ -133,6 +137,9 @@ class Library:
             L.osqp_gb300_solve_stats.argtypes = [PSolver, C.POINTER(I), C.POINTER(C.c_longlong),
                                                  C.POINTER(C.c_double), C.POINTER(I)]
             L.osqp_gb300_solve_stats.restype = I
+        if hasattr(L, "osqp_gb300_precond_blocks"):
+            L.osqp_gb300_precond_blocks.argtypes = [PSolver, C.POINTER(F)]
+            L.osqp_gb300_precond_blocks.restype = I
 
     def default_settings(self):
         s = self.Settings()
@@ -239,6 +246,18 @@ class OSQP:
         ms = C.c_double()
         self.L.lib.osqp_gb300_solve_stats(self._solver, C.byref(it), C.byref(pcg), C.byref(ms), C.byref(form))
         return {"admm_iter": it.value, "pcg_iter": pcg.value, "kernel_ms": ms.value, "grid": form.value}
+
+    def precond_blocks(self) -> np.ndarray:
+        """Block-Jacobi blocks of M^-1 (cg_precond = 2) as an array of shape
+        (ceil(n / 32), 32, 32); empty when the solver has none."""
+        L = self.L
+        cnt = int(L.lib.osqp_gb300_precond_blocks(self._solver, None))
+        out = np.zeros(cnt, dtype=L.np_float)
+        if cnt:
+            got = int(L.lib.osqp_gb300_precond_blocks(self._solver, _ptr(out, L.F)))
+            if got != cnt:
+                raise RuntimeError("osqp_gb300_precond_blocks failed")
+        return out.reshape(-1, 32, 32)
 
     def settings(self):
         return self._solver.contents.settings.contents

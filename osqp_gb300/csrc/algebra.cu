@@ -792,10 +792,22 @@ struct GbPcg {
 
 static const char* ls_name(LinSysSolver* self) {
   GbPcg* s = (GbPcg*)self;
+  if (s->ds.cg_precond == kPrecondBlockDiagonal) return "GB300 reduced-KKT PCG - Block-diagonal preconditioner";
   return s->ds.cg_precond ? "GB300 reduced-KKT PCG - Diagonal preconditioner" : "GB300 reduced-KKT PCG - No preconditioner";
+}
+// Block-Jacobi storage, allocated when cg_precond = 2 is first asked for.
+static int ls_ensure_blocks(GbPcg* s) {
+  if (s->pr.Binv || s->ds.cg_precond != kPrecondBlockDiagonal) return 0;
+  T* p = nullptr;
+  if (cudaMalloc((void**)&p, sizeof(T) * block_precond_elems(s->n)) != cudaSuccess) return 1;
+  s->pr.Binv = p;
+  return 0;
 }
 static void ls_precond(GbPcg* s) {
   k_ls_precond<<<ew_blocks(s->n), kEwThreads, 0, stream()>>>(s->pr, s->ds.sigma, s->rho, s->rho_vec, s->ds.cg_precond);
+  if (s->ds.cg_precond == kPrecondBlockDiagonal && s->pr.Binv && s->n > 0)
+    k_block_precond<T><<<block_precond_grid(s->n), kBlockPrecondThreads, 0, stream()>>>(s->pr, s->ds.sigma, s->rho,
+                                                                                       s->rho_vec);
 }
 static OSQPInt ls_solve(LinSysSolver* self, OSQPVectorf* b, OSQPInt admm_iter) {
   GbPcg* s = (GbPcg*)self;
@@ -819,7 +831,16 @@ static void ls_update_settings(LinSysSolver* self, const OSQPSettings* st) {
   s->ds.cg_max_iter = st->cg_max_iter;
   s->ds.cg_tol_reduction = st->cg_tol_reduction;
   s->ds.cg_tol_fraction = st->cg_tol_fraction;
-  if (s->ds.cg_precond != (int)st->cg_precond) { s->ds.cg_precond = (int)st->cg_precond; ls_precond(s); }
+  if (s->ds.cg_precond != (int)st->cg_precond) {
+    const int before = s->ds.cg_precond;
+    s->ds.cg_precond = (int)st->cg_precond;
+    if (ls_ensure_blocks(s)) {
+      // no room for the blocks: the solver keeps its previous preconditioner
+      fprintf(stderr, "osqp_gb300 linsys: no device memory for the block-diagonal preconditioner\n");
+      s->ds.cg_precond = before;
+    }
+    ls_precond(s);
+  }
 }
 static void ls_warm_start(LinSysSolver* self, const OSQPVectorf* x) {
   GbPcg* s = (GbPcg*)self;
@@ -830,6 +851,7 @@ static void ls_free(LinSysSolver* self) {
   GbPcg* s = (GbPcg*)self;
   if (!s) return;
   if (s->arena) cudaFree(s->arena);
+  if (s->pr.Binv) cudaFree(s->pr.Binv);
   free(s);
 }
 static OSQPInt ls_update_matrices(LinSysSolver* self, const OSQPMatrix*, const OSQPInt*, OSQPInt, const OSQPMatrix*,
@@ -891,6 +913,8 @@ extern "C" OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** sp, const OSQP
   pr.xp = (T*)(a + o_vn[0]); pr.r = (T*)(a + o_vn[1]); pr.p0 = (T*)(a + o_vn[2]); pr.p1 = (T*)(a + o_vn[3]);
   pr.Kp = (T*)(a + o_vn[4]); pr.yv = (T*)(a + o_vn[5]); pr.rhs = (T*)(a + o_vn[6]); pr.Minv = (T*)(a + o_vn[7]);
   pr.t = (T*)(a + o_t);
+  pr.Arow_g = pr.A.rowptr; pr.Acol_g = pr.A.col; pr.Aval_g = pr.A.val;
+  if (ls_ensure_blocks(s)) { ls_free(&s->base); return OSQP_LINSYS_SOLVER_INIT_ERROR; }
   s->d_st = (SolverScalars*)(a + o_st);
   pr.st = s->d_st;
   s->bar = (unsigned*)(a + o_bar); s->err = (int*)(s->bar + 4);
@@ -945,10 +969,12 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 static void* g_noalloc_addr[64];   // device address of g_noalloc_scratch, per device
 
 // Bytes of scratch a solve with n variables and m constraints needs: eight
-// n-vectors and one m-vector, each on a 256-byte boundary.
-static size_t noalloc_bytes(long long n, long long m) {
+// n-vectors and one m-vector, each on a 256-byte boundary, then the
+// block-Jacobi blocks when `blocks` is set.
+static size_t noalloc_bytes(long long n, long long m, bool blocks) {
   auto r = [](size_t b) { return (b + 255) & ~size_t(255); };
-  return 8 * r(sizeof(T) * (size_t)(n > 0 ? n : 1)) + r(sizeof(T) * (size_t)(m > 0 ? m : 1));
+  return 8 * r(sizeof(T) * (size_t)(n > 0 ? n : 1)) + r(sizeof(T) * (size_t)(m > 0 ? m : 1)) +
+         (blocks ? r(sizeof(T) * block_precond_elems(n)) : 0);
 }
 
 __global__ void __launch_bounds__(kLsBlockThreads, 1)
@@ -983,7 +1009,8 @@ extern "C" OSQPInt osqp_gb300_linsys_solve_noalloc(const OSQPMatrix* P, const OS
   if (!P || !A || !settings || !b) return OSQP_DATA_VALIDATION_ERROR;
   const int n = P->n, m = A->m;
   if (b->length != n + m || A->n != n) return OSQP_DATA_VALIDATION_ERROR;
-  const size_t need = noalloc_bytes(n, m);
+  const bool blocks = settings->cg_precond == (osqp_precond_type)kPrecondBlockDiagonal;
+  const size_t need = noalloc_bytes(n, m, blocks);
   if (need > kNoAllocScratchBytes) {
     fprintf(stderr,
             "osqp_gb300_linsys_solve_noalloc: n=%d, m=%d needs %zu bytes of scratch; the fixed maximum is %zu bytes\n",
@@ -1014,6 +1041,8 @@ extern "C" OSQPInt osqp_gb300_linsys_solve_noalloc(const OSQPMatrix* P, const OS
   pr.xp = (T*)(base + 0 * vn); pr.r = (T*)(base + 1 * vn); pr.p0 = (T*)(base + 2 * vn); pr.p1 = (T*)(base + 3 * vn);
   pr.Kp = (T*)(base + 4 * vn); pr.yv = (T*)(base + 5 * vn); pr.rhs = (T*)(base + 6 * vn); pr.Minv = (T*)(base + 7 * vn);
   pr.t = (T*)(base + 8 * vn);
+  pr.Arow_g = pr.A.rowptr; pr.Acol_g = pr.A.col; pr.Aval_g = pr.A.val;
+  pr.Binv = blocks ? (T*)(base + 8 * vn + r(sizeof(T) * (size_t)(m > 0 ? m : 1))) : nullptr;
   DevSettings d;
   memset(&d, 0, sizeof(d));
   d.sigma = settings->sigma;

@@ -68,6 +68,7 @@ struct BatchInst {
   int pt_off, a_off;    // offsets of the QP's triu-P and A entries (input order)
   int kktL, PL, AL, AtL;
   int Pdiag_only;       // P holds exactly its full diagonal
+  int blk_off;          // first 32 x 32 block-Jacobi block of the QP (cg_precond = 2)
 };
 
 template <typename TT>
@@ -81,6 +82,7 @@ struct BatchArrays {
   int* ctype;
   SolverScalars* st;
   const BatchInst* inst;
+  TT* Binv;             // block-Jacobi blocks of every QP (nullptr unless cg_precond = 2)
 
   __device__ DevProblem<TT> problem(int k) const {
     const BatchInst b = inst[k];
@@ -103,6 +105,8 @@ struct BatchArrays {
     pr.pcert = vm[13] + p; pr.Et = vm[14] + p;
     pr.ctype = ctype + p;
     pr.st = st + k;
+    pr.Binv = Binv ? Binv + (size_t)b.blk_off * kPrecondBlock * kPrecondBlock : nullptr;
+    pr.Arow_g = pr.A.rowptr; pr.Acol_g = Acol; pr.Aval_g = Aval;
     return pr;
   }
 };
@@ -243,8 +247,9 @@ __device__ __forceinline__ bool stage_problem(DevProblem<TT>& pr, const Spans& s
 // estimated work: a row costs its entries plus 4 x (lanes per row), the
 // entries a sub-warp could have processed in the row's fixed per-row work.
 // n-space rows cost their P and A' entries, m-space rows their A entries.
+// n-slice boundaries are rounded down to multiples of `align`.
 template <typename TT>
-__device__ Spans cluster_spans(const DevProblem<TT>& pr, int kktL, int r, int c) {
+__device__ Spans cluster_spans(const DevProblem<TT>& pr, int kktL, int r, int c, int align) {
   Spans sp;
   auto cut = [&](const int* r1, const int* r2, int rows, long long per_row, long long target) {
     int lo = 0, hi = rows;   // first row i with cost(i) >= target
@@ -258,8 +263,8 @@ __device__ Spans cluster_spans(const DevProblem<TT>& pr, int kktL, int r, int c)
   };
   const long long wn = 4LL * kktL;
   const long long Fn = (pr.P.rowptr[pr.n] - pr.P.rowptr[0]) + (pr.At.rowptr[pr.n] - pr.At.rowptr[0]) + wn * pr.n;
-  sp.nlo = r == 0 ? 0 : cut(pr.P.rowptr, pr.At.rowptr, pr.n, wn, Fn * r / c);
-  sp.nhi = r == c - 1 ? pr.n : cut(pr.P.rowptr, pr.At.rowptr, pr.n, wn, Fn * (r + 1) / c);
+  sp.nlo = r == 0 ? 0 : cut(pr.P.rowptr, pr.At.rowptr, pr.n, wn, Fn * r / c) / align * align;
+  sp.nhi = r == c - 1 ? pr.n : cut(pr.P.rowptr, pr.At.rowptr, pr.n, wn, Fn * (r + 1) / c) / align * align;
   if (pr.m) {
     const long long wm = 4LL * pr.A.lanes;
     const long long Fm = (pr.A.rowptr[pr.m] - pr.A.rowptr[0]) + wm * pr.m;
@@ -285,7 +290,9 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   bool staged = false;
   if (mode == kModeSolve && dsm_bytes > 0) {
     if constexpr (std::is_same<G, ClusterGroup>::value) {
-      g.sp = cluster_spans(pv, B.inst[k].kktL, (int)g.rank, (int)g.size);
+      // block-Jacobi needs each block of r in one CTA: n-slices start on block boundaries
+      g.sp = cluster_spans(pv, B.inst[k].kktL, (int)g.rank, (int)g.size,
+                           s.cg_precond == kPrecondBlockDiagonal ? kPrecondBlock : 1);
       g.sliced = true;
     }
     staged = stage_problem(pv, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, 1, stage_mat != 0, stage_mat == 2);
@@ -581,6 +588,7 @@ static int env_int(const char* name, int dflt) {
 struct OSQPBatch_ {
   int count, device;
   long long nsum, msum, nnzT, nnzA, nnzPf;
+  size_t binv_elems;    // block-Jacobi storage (0 unless cg_precond = 2)
   cudaStream_t stream;
   cudaEvent_t ev0, ev1, evu;
   int upd_pending;
@@ -766,10 +774,12 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   }
   b->inst.resize(count);
   std::vector<int> pp_off(count), work(count);
-  long long no = 0, mo = 0, pto = 0, ao = 0, co = 0;
+  long long no = 0, mo = 0, pto = 0, ao = 0, co = 0, blk = 0;
   for (int k = 0; k < count; k++) {
     BatchInst& I = b->inst[k];
     I.n = hn[k]; I.m = hm[k]; I.n_off = (int)no; I.m_off = (int)mo; I.pt_off = (int)pto; I.a_off = (int)ao;
+    I.blk_off = (int)blk;
+    blk += (hn[k] + kPrecondBlock - 1) / kPrecondBlock;
     pp_off[k] = (int)co;
     const int nT = hPp[co + hn[k]], nA = hAp[co + hn[k]];
     no += hn[k]; mo += hm[k]; pto += nT; ao += nA; co += hn[k] + 1;
@@ -777,6 +787,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   }
   if (pto > INT32_MAX / 2 || ao > INT32_MAX || no > INT32_MAX / 2) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
   b->nsum = nsum; b->msum = msum; b->nnzT = pto; b->nnzA = ao;
+  b->binv_elems = b->ds.cg_precond == kPrecondBlockDiagonal ? (size_t)blk * kPrecondBlock * kPrecondBlock : 0;
   // diagonal count of P (host scan of the triu pattern) -> full-P size
   std::vector<OSQPInt> hPi(pto > 0 ? pto : 1);
   if (pto && cudaMemcpy(hPi.data(), Pi, sizeof(OSQPInt) * pto, cudaMemcpyDefault) != cudaSuccess) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
@@ -831,6 +842,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   size_t o_order2 = pl.take(sizeof(int) * count);
   size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 2);
   size_t o_sq = pl.take(sizeof(T) * nsum), o_sl = pl.take(sizeof(T) * msum), o_su = pl.take(sizeof(T) * msum);
+  size_t o_binv = pl.take(sizeof(T) * b->binv_elems);
   {
     // admission by free device memory: refuse (rather than fail part-way)
     // when the pool and the set-up scratch would not fit
@@ -853,6 +865,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   B.Aval = (T*)(a + o_Aval); B.Araw = (T*)(a + o_Araw); B.Atval = (T*)(a + o_Atval);
   for (int k = 0; k < 16; k++) { B.vn[k] = (T*)(a + o_vn[k]); B.vm[k] = (T*)(a + o_vm[k]); }
   B.ctype = (int*)(a + o_ctype); B.st = (SolverScalars*)(a + o_st);
+  B.Binv = b->binv_elems ? (T*)(a + o_binv) : nullptr;
   b->d_inst = (BatchInst*)(a + o_inst); B.inst = b->d_inst;
   b->d_order = (int*)(a + o_order);
   b->d_queue = (int*)(a + o_misc); b->d_flag = b->d_queue + 1;
@@ -1053,12 +1066,13 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
   BatchArrays<T>& B = b->B;
   const size_t vbytes = sizeof(T) * 16 * (size_t)(b->nsum + b->msum);
   const size_t sbytes = sizeof(SolverScalars) * (size_t)b->count;
+  const size_t bbytes = sizeof(T) * b->binv_elems;   // block-Jacobi blocks follow rho
   char* snap = nullptr;
   int* dbuf = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int rc = 0;
   int best = b->per_lane;
-  if (cudaMallocAsync((void**)&snap, vbytes + sbytes, s) != cudaSuccess ||
+  if (cudaMallocAsync((void**)&snap, vbytes + sbytes + bbytes, s) != cudaSuccess ||
       cudaMallocAsync((void**)&dbuf, sizeof(int) * (2 * (size_t)ns + 4), s) != cudaSuccess ||
       cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = OSQP_MEM_ALLOC_ERROR;
   size_t off = 0;
@@ -1067,6 +1081,7 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
     cudaMemcpyAsync(snap + off, B.vm[k], sizeof(T) * b->msum, cudaMemcpyDeviceToDevice, s); off += sizeof(T) * b->msum;
   }
   if (!rc) cudaMemcpyAsync(snap + off, B.st, sbytes, cudaMemcpyDeviceToDevice, s);
+  if (!rc && bbytes) cudaMemcpyAsync(snap + off + sbytes, B.Binv, bbytes, cudaMemcpyDeviceToDevice, s);
   if (!rc) cudaMemcpyAsync(dbuf, sample.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s);
   LaunchBufs lb{dbuf, ns, dbuf + 2 * (size_t)ns, dbuf + ns};
   float best_ms = 1e30f, default_ms = 1e30f;
@@ -1101,6 +1116,7 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
       cudaMemcpyAsync(B.vm[k], snap + off, sizeof(T) * b->msum, cudaMemcpyDeviceToDevice, s); off += sizeof(T) * b->msum;
     }
     cudaMemcpyAsync(B.st, snap + off, sbytes, cudaMemcpyDeviceToDevice, s);
+    if (bbytes) cudaMemcpyAsync(B.Binv, snap + off + sbytes, bbytes, cudaMemcpyDeviceToDevice, s);
     cudaFreeAsync(snap, s);
   }
   if (dbuf) cudaFreeAsync(dbuf, s);

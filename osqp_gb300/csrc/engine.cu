@@ -257,6 +257,16 @@ struct OSQPWorkspace_ {
   void* polish;           // polish workspace (gb_polish.cu)
 };
 
+// Block-Jacobi storage, allocated when cg_precond = 2 is first asked for
+// (set-up or a settings update) and kept until cleanup.
+static int ensure_block_precond(OSQPWorkspace* w) {
+  if (w->pr.Binv || w->ds.cg_precond != kPrecondBlockDiagonal) return 0;
+  T* p = nullptr;
+  if (cudaMalloc((void**)&p, sizeof(T) * block_precond_elems(w->n)) != cudaSuccess) return OSQP_MEM_ALLOC_ERROR;
+  w->pr.Binv = p;
+  return 0;
+}
+
 // FP64 polish stage (polish.cu); returns >0 on a hard failure.
 int gb_polish_run(OSQPSolver* solver);
 void gb_polish_free(void* p);
@@ -507,6 +517,7 @@ static void free_workspace(OSQPWorkspace* w) {
   if (!w) return;
   if (w->polish) { gb_polish_free(w->polish); w->polish = NULL; }
   if (w->arena) cudaFree(w->arena);
+  if (w->pr.Binv) cudaFree(w->pr.Binv);
   if (w->h_x) cudaFreeHost(w->h_x);
   if (w->h_st) cudaFreeHost(w->h_st);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -614,6 +625,8 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   pr.t = vm[11]; pr.yo = vm[12]; pr.pcert = vm[13]; pr.Et = vm[14];
   pr.ctype = (int*)(b + o_ctype);
   pr.st = (SolverScalars*)(b + o_st);
+  pr.Arow_g = pr.A.rowptr; pr.Acol_g = pr.A.col; pr.Aval_g = pr.A.val;
+  pr.Binv = nullptr;
   w->bar = (unsigned int*)(b + o_bar);
   w->err = (int*)(b + o_err);
   w->flag = w->err + 1;
@@ -691,6 +704,7 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   if (st->adaptive_rho == OSQP_ADAPTIVE_RHO_UPDATE_KKT_ERROR && st->adaptive_rho_interval == 0)
     st->adaptive_rho_interval = 1;
   w->ds = make_dev_settings(st);
+  if (ensure_block_precond(w)) { osqp_cleanup(solver); return OSQP_MEM_ALLOC_ERROR; }
 
   if (cudaMallocHost((void**)&w->h_st, sizeof(SolverScalars)) != cudaSuccess) { osqp_cleanup(solver); return OSQP_MEM_ALLOC_ERROR; }
   int rc = launch_setup(w, 0);
@@ -865,6 +879,14 @@ static void reset_info(OSQPInfo* info) {
 
 static const int kEwBlocks = 296, kEwThreads = 256;
 
+// Preconditioner refresh driven by the host: the Jacobi diagonal and, with
+// cg_precond = 2, the blocks of the block-Jacobi one.
+static void refresh_precond(OSQPWorkspace* w, cudaStream_t s, double rho, int rho_is_vec) {
+  k_precond<T><<<kEwBlocks, kEwThreads, 0, s>>>(w->pr, w->ds.sigma, rho, rho_is_vec, w->ds.cg_precond);
+  if (w->ds.cg_precond == kPrecondBlockDiagonal && w->pr.Binv)
+    k_block_precond<T><<<block_precond_grid(w->n), kBlockPrecondThreads, 0, s>>>(w->pr, w->ds.sigma, rho, rho_is_vec);
+}
+
 extern "C" OSQPInt osqp_update_data_vec(OSQPSolver* solver, const OSQPFloat* q_new, const OSQPFloat* l_new,
                                         const OSQPFloat* u_new) {
   if (!solver || !solver->work) return OSQP_WORKSPACE_NOT_INIT_ERROR;
@@ -911,8 +933,7 @@ extern "C" OSQPInt osqp_update_data_vec(OSQPSolver* solver, const OSQPFloat* q_n
       k_rho_vec<T><<<kEwBlocks, kEwThreads, 0, s>>>(w->pr, w->h_st->rho, (double)OSQP_INFTY, 1, w->flag);
       GB_TRY(cudaMemcpyAsync(&changed, w->flag, sizeof(int), cudaMemcpyDeviceToHost, s));
       GB_TRY(cudaStreamSynchronize(s));
-      if (changed)
-        k_precond<T><<<kEwBlocks, kEwThreads, 0, s>>>(w->pr, w->ds.sigma, w->h_st->rho, 1, w->ds.cg_precond);
+      if (changed) refresh_precond(w, s, w->h_st->rho, 1);
     }
   }
   GB_TRY(cudaStreamSynchronize(s));
@@ -962,7 +983,7 @@ extern "C" OSQPInt osqp_update_rho(OSQPSolver* solver, OSQPFloat rho_new) {
   w->h_st->rho_inv = 1.0 / rho;
   GB_TRY(cudaMemcpyAsync(w->pr.st, w->h_st, sizeof(SolverScalars), cudaMemcpyHostToDevice, s));
   if (solver->settings->rho_is_vec) k_rho_vec<T><<<kEwBlocks, kEwThreads, 0, s>>>(w->pr, rho, (double)OSQP_INFTY, 0, w->flag);
-  k_precond<T><<<kEwBlocks, kEwThreads, 0, s>>>(w->pr, w->ds.sigma, rho, solver->settings->rho_is_vec, w->ds.cg_precond);
+  refresh_precond(w, s, rho, solver->settings->rho_is_vec);
   GB_TRY(cudaStreamSynchronize(s));
   return 0;
 }
@@ -1011,6 +1032,7 @@ extern "C" OSQPInt osqp_update_settings(OSQPSolver* solver, const OSQPSettings* 
   OSQPSettings* s = solver->settings;
   OSQPWorkspace* w = solver->work;
   const int precond_changed = s->cg_precond != ns->cg_precond;
+  const osqp_precond_type precond_before = s->cg_precond;
   s->profiler_level = ns->profiler_level; s->verbose = ns->verbose; s->warm_starting = ns->warm_starting;
   s->polishing = ns->polishing; s->alpha = ns->alpha;
   s->cg_max_iter = ns->cg_max_iter; s->cg_tol_reduction = ns->cg_tol_reduction;
@@ -1023,9 +1045,15 @@ extern "C" OSQPInt osqp_update_settings(OSQPSolver* solver, const OSQPSettings* 
   w->ds = make_dev_settings(s);
   if (precond_changed) {
     cudaSetDevice(w->device);
+    if (ensure_block_precond(w)) {
+      // no room for the blocks: keep the previous preconditioner
+      s->cg_precond = precond_before;
+      w->ds = make_dev_settings(s);
+      return OSQP_MEM_ALLOC_ERROR;
+    }
     GB_TRY(cudaMemcpyAsync(w->h_st, w->pr.st, sizeof(SolverScalars), cudaMemcpyDeviceToHost, w->stream));
     GB_TRY(cudaStreamSynchronize(w->stream));
-    k_precond<T><<<kEwBlocks, kEwThreads, 0, w->stream>>>(w->pr, w->ds.sigma, w->h_st->rho, s->rho_is_vec, w->ds.cg_precond);
+    refresh_precond(w, w->stream, w->h_st->rho, s->rho_is_vec);
     GB_TRY(cudaStreamSynchronize(w->stream));
   }
   return 0;
@@ -1040,6 +1068,20 @@ extern "C" OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter
   if (kernel_ms) *kernel_ms = w->last_kernel_ms;
   if (grid_form) *grid_form = w->use_grid ? 1 : (w->cluster > 1 ? w->cluster : 0);
   return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_precond_blocks(OSQPSolver* solver, OSQPFloat* out) {
+  if (!solver || !solver->work) return 0;
+  OSQPWorkspace* w = solver->work;
+  if (w->ds.cg_precond != kPrecondBlockDiagonal || !w->pr.Binv) return 0;
+  const size_t cnt = block_precond_elems(w->n);
+  if (out) {
+    cudaSetDevice(w->device);
+    if (cudaMemcpyAsync(out, w->pr.Binv, sizeof(T) * cnt, cudaMemcpyDefault, w->stream) != cudaSuccess ||
+        cudaStreamSynchronize(w->stream) != cudaSuccess)
+      return 0;
+  }
+  return (OSQPInt)cnt;
 }
 
 // The workspace as the polish stage sees it.

@@ -99,7 +99,139 @@ struct DevProblem {
   T *xo, *yo, *pcert, *dcert;   // stored solution (unscaled)
   T *Dt, *Et;                   // scaling scratch
   SolverScalars* st;            // persistent scalars
+  // Block-Jacobi preconditioner (cg_precond = 2): the inverted 32 x 32
+  // diagonal blocks of K (nullptr when not allocated), and A's CSR arrays in
+  // global memory, which shared-memory staging never redirects
+  T* Binv;
+  const int *Arow_g, *Acol_g;
+  const T* Aval_g;
 };
+
+// ---------------------------------------------------------------------------
+// Block-Jacobi preconditioner (cg_precond = 2).  The reference's PCG has the
+// diagonal one only (cuda_pcg.cu:211-266); this is the block form of it.  M
+// is the block diagonal of K = P + sigma I + A' R A with 32-variable blocks
+// [32 b, 32 b + 32) (the last one shorter when 32 does not divide n).  Block
+// b of M^-1 is stored at Binv + 1024 b, entry (j, i) at 32 j + i: the inverse
+// is symmetric, so the lanes of a warp applying it read one row with one
+// coalesced load per column.
+// ---------------------------------------------------------------------------
+constexpr int kPrecondBlock = 32;
+enum : int { kPrecondNone = 0, kPrecondDiagonal = 1, kPrecondBlockDiagonal = 2 };
+
+// Elements of M^-1 storage for n variables.
+__host__ __device__ inline size_t block_precond_elems(long long n) {
+  return (size_t)((n + kPrecondBlock - 1) / kPrecondBlock) * kPrecondBlock * kPrecondBlock;
+}
+
+// Block b of M^-1, computed by one whole warp (b warp-uniform).  Lane i forms
+// row i of the block of K in FP64 (P entries, then the A' R A terms in
+// ascending constraint order, then sigma on the diagonal), then the warp
+// inverts the block in place by symmetric Gauss-Jordan sweeps (the sweep
+// operator; sweeping every pivot leaves -K^-1):
+//   d = 1 / a_kk;  a_ij -= (a_ik a_kj) d  (i, j != k);  a_ik = a_ik d;  a_kk = -d
+// with row k broadcast by shuffles.  Each product is formed alike for (i, j)
+// and (j, i), so the block stays symmetric.  A pivot that is not positive and
+// finite (a block that is not numerically positive definite) leaves the
+// whole block diagonal, 1 / K_ii, as the Jacobi preconditioner would.
+// P and A' rows of the block are read through their (possibly staged) CSR;
+// rows of A through the global arrays, any of which a block may touch.
+template <typename T>
+__device__ __noinline__ void kkt_block_inverse(CSR<T> P, CSR<T> At, const int* Arow, const int* Acol, const T* Aval,
+                                               const T* rho_vec, T* Binv, int n, int b, double sig, double rho) {
+  const int lane = threadIdx.x & 31;
+  const int i0 = b * kPrecondBlock, nb = min(kPrecondBlock, n - i0);
+  const int i = i0 + lane;
+  double a[kPrecondBlock];
+#pragma unroll
+  for (int j = 0; j < kPrecondBlock; j++) a[j] = (j == lane) ? 1.0 : 0.0;   // padding rows: identity
+  if (lane < nb) {
+#pragma unroll
+    for (int j = 0; j < kPrecondBlock; j++) a[j] = 0.0;
+    const int* col; const T* val; int kb, ke;
+    row_ptrs(P, i, true, col, val, kb, ke);
+    for (int k = kb; k < ke; k++) {
+      const int c = col[k] - i0;
+      const double v = (double)val[k];
+#pragma unroll
+      for (int j = 0; j < kPrecondBlock; j++) if (j == c) a[j] += v;
+    }
+    row_ptrs(At, i, true, col, val, kb, ke);
+    for (int e = kb; e < ke; e++) {
+      const int k = col[e];
+      const double aki = (double)val[e];
+      const double rk = rho_vec ? (double)rho_vec[k] : rho;
+      // entries of row k of A in columns [i0, i0 + nb): first one by bisection
+      int lo = Arow[k], hi = Arow[k + 1];
+      const int end = hi;
+      while (lo < hi) { const int mid = (lo + hi) >> 1; if (Acol[mid] < i0) lo = mid + 1; else hi = mid; }
+      for (int f = lo; f < end; f++) {
+        const int c = Acol[f] - i0;
+        if (c >= nb) break;
+        const double w = rk * (aki * (double)Aval[f]);
+#pragma unroll
+        for (int j = 0; j < kPrecondBlock; j++) if (j == c) a[j] += w;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kPrecondBlock; j++) if (j == lane) a[j] += sig;
+  }
+  double d0 = 1.0;   // K_ii
+#pragma unroll
+  for (int j = 0; j < kPrecondBlock; j++) if (j == lane) d0 = a[j];
+  bool ok = true;
+  for (int k = 0; k < nb; k++) {
+    double aik = 0.0;
+#pragma unroll
+    for (int j = 0; j < kPrecondBlock; j++) if (j == k) aik = a[j];
+    const double piv = __shfl_sync(0xffffffffu, aik, k);
+    if (!(piv > 0.0) || !isfinite(piv)) { ok = false; break; }   // warp-uniform
+    const double d = 1.0 / piv;
+#pragma unroll
+    for (int j = 0; j < kPrecondBlock; j++) {
+      const double akj = __shfl_sync(0xffffffffu, a[j], k);
+      if (j == k) a[j] = (lane == k) ? -d : aik * d;
+      else a[j] = (lane == k) ? akj * d : a[j] - (aik * akj) * d;
+    }
+  }
+  // padding rows and columns (past n) are stored as zeros
+  T* Bb = Binv + (size_t)b * kPrecondBlock * kPrecondBlock;
+#pragma unroll
+  for (int j = 0; j < kPrecondBlock; j++)
+    Bb[j * kPrecondBlock + lane] = (lane >= nb || j >= nb) ? T(0)
+                                   : ok ? (T)(-a[j]) : (j == lane ? (T)(1.0 / d0) : T(0));
+}
+
+// (M^-1 r)_i for the block holding i; r must hold the whole block.  Fixed
+// summation order (ascending j), whatever thread computes it.
+template <typename T>
+__device__ __forceinline__ T block_apply(const T* __restrict__ Binv, const T* r, int n, int i) {
+  const int b0 = i & ~(kPrecondBlock - 1), li = i & (kPrecondBlock - 1);
+  const T* Bb = Binv + (size_t)b0 * kPrecondBlock;
+  const int nb = min(kPrecondBlock, n - b0);
+  T acc = T(0);
+#pragma unroll 8
+  for (int j = 0; j < nb; j++) acc = fma(Bb[j * kPrecondBlock + li], r[b0 + j], acc);
+  return acc;
+}
+
+// The block build as its own launch (preconditioner refreshes the host
+// drives: rho and settings updates): one warp per block.
+constexpr int kBlockPrecondThreads = 256;
+template <typename T>
+__global__ void __launch_bounds__(kBlockPrecondThreads) k_block_precond(DevProblem<T> pr, double sigma, double rho,
+                                                                        int rho_is_vec) {
+  const int nblk = (pr.n + kPrecondBlock - 1) / kPrecondBlock;
+  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), nw = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int b = w; b < nblk; b += nw)
+    kkt_block_inverse<T>(pr.P, pr.At, pr.Arow_g, pr.Acol_g, pr.Aval_g, rho_is_vec ? pr.rho_vec : nullptr, pr.Binv,
+                         pr.n, b, sigma, rho);
+}
+inline int block_precond_grid(int n) {
+  const long long warps = (n + kPrecondBlock - 1) / kPrecondBlock;
+  const long long blocks = (warps * 32 + kBlockPrecondThreads - 1) / kBlockPrecondThreads;
+  return (int)(blocks < 1 ? 1 : (blocks > 4096 ? 4096 : blocks));
+}
 
 template <typename T> __device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
 template <typename T> __device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
@@ -295,7 +427,8 @@ struct Solver {
     });
   }
 
-  // Jacobi preconditioner M = sigma + diag(P) + diag(A' R A) (cuda_pcg.cu:211-266)
+  // Jacobi preconditioner M = sigma + diag(P) + diag(A' R A) (cuda_pcg.cu:211-266),
+  // and with cg_precond = 2 the inverted blocks of the block-Jacobi one
   template <typename G>
   __device__ void update_precond(G& g) {
     // local copies: hot loops keep the pointers in registers instead of
@@ -316,6 +449,15 @@ struct Solver {
       if (!vec) d *= rho;
       pr.Minv[i] = T(1) / (sig + pr.P.val[pr.Pdiag[i]] + d);
     });
+    if (s.cg_precond == kPrecondBlockDiagonal && pr.Binv) {
+      // one warp per block, over the blocks of this CTA's part of the n-space
+      // (a sliced cluster's spans start on block boundaries)
+      const Rng rg = span_n(g, pr.n);
+      const int b_lo = rg.lo / kPrecondBlock, b_hi = (rg.hi + kPrecondBlock - 1) / kPrecondBlock;
+      for (int b = b_lo + g.w0(); b < b_hi; b += g.ws())
+        kkt_block_inverse<T>(pr.P, pr.At, pr.Arow_g, pr.Acol_g, pr.Aval_g, vec ? pr.rho_vec : nullptr, pr.Binv,
+                             pr.n, b, s.sigma, sc->rho);
+    }
   }
 
   template <typename G>
@@ -471,6 +613,7 @@ struct Solver {
   // and thr is the smallest float above eps.  Same recurrence and phases as
   // pcg_core; barriers per iteration: 4 instead of 6.
   // ---------------------------------------------------------------------
+  template <bool BLK>
   __device__ int pcg_core_block32(BlockGroup& g, double eps, float sig, float rho_s) {
     const DevProblem<float> pr = this->pr;
     const DevSettings s = this->s;
@@ -484,17 +627,32 @@ struct Solver {
     int par = 0;
     // Phase I: r = K xp - rhs, yv = M^-1 r, p = -yv, rTy, ||r||
     float* p = sc->p_parity ? pr.p1 : pr.p0;
+    // BLK (block-Jacobi): M^-1 r needs the whole block of r, so it is a
+    // second pass after a barrier (one more barrier per iteration).  A
+    // separate instantiation keeps the Jacobi loop's registers as they were.
+    constexpr bool blk = BLK;
     Acc<float> rty;
     float rn = 0.f;
     kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return xp[c]; }, [&](int c) { return m ? pr.t[c] : 0.f; },
       [&](int i, float pv, float av) {
         const float kx = sig * xp[i] + pv + av;
         const float r = kx - pr.rhs[i];
-        const float yv = pr.Minv[i] * r;
-        pr.r[i] = r; pr.yv[i] = yv; p[i] = -yv;
-        rty.add_prod(yv, r);
+        pr.r[i] = r;
         rn = tmax(rn, fabsf(r));
+        if constexpr (!blk) {
+          const float yv = pr.Minv[i] * r;
+          pr.yv[i] = yv; p[i] = -yv;
+          rty.add_prod(yv, r);
+        }
       });
+    if constexpr (blk) {
+      __syncthreads();
+      for_n(g, n, [&](int i) {
+        const float yv = block_apply(pr.Binv, pr.r, n, i);
+        pr.yv[i] = yv; p[i] = -yv;
+        rty.add_prod(yv, pr.r[i]);
+      });
+    }
     g.reduce1(rty, rn, par);
     int it = 0;
     bool cont = rn >= thr && 0 < cg_max;
@@ -524,11 +682,21 @@ struct Solver {
         xp[i] = xp[i] + at * p[i];
         const float r = pr.r[i] + at * pr.Kp[i];
         pr.r[i] = r;
-        const float yv = pr.Minv[i] * r;
-        pr.yv[i] = yv;
-        rty_new.add_prod(yv, r);
         rn2 = tmax(rn2, fabsf(r));
+        if constexpr (!blk) {
+          const float yv = pr.Minv[i] * r;
+          pr.yv[i] = yv;
+          rty_new.add_prod(yv, r);
+        }
       });
+      if constexpr (blk) {
+        __syncthreads();
+        for_n(g, n, [&](int i) {
+          const float yv = block_apply(pr.Binv, pr.r, n, i);
+          pr.yv[i] = yv;
+          rty_new.add_prod(yv, pr.r[i]);
+        });
+      }
       g.reduce1(rty_new, rn2, par);
       const float bt = df_div(rty_new.hi, rty_new.lo, rty.hi, rty.lo);
       rty = rty_new;
@@ -556,8 +724,14 @@ struct Solver {
   // ---------------------------------------------------------------------
   template <typename G>
   __device__ int pcg_core(G& g, double eps, T sig, T rho_s) {
+    const bool blk = s.cg_precond == kPrecondBlockDiagonal && pr.Binv;
     if constexpr (std::is_same<T, float>::value && std::is_same<G, BlockGroup>::value)
-      return pcg_core_block32(g, eps, sig, rho_s);
+      return blk ? pcg_core_block32<true>(g, eps, sig, rho_s) : pcg_core_block32<false>(g, eps, sig, rho_s);
+    else
+      return pcg_core_any(g, eps, sig, rho_s, blk);
+  }
+  template <typename G>
+  __device__ int pcg_core_any(G& g, double eps, T sig, T rho_s, const bool blk) {
     // local copies: hot loops keep the pointers in registers instead of
     // re-reading them through `this` after every store
     const DevProblem<T> pr = this->pr;
@@ -575,17 +749,30 @@ struct Solver {
     T* bT = bcast_slots<T>(gs);   // [0] alpha  [1] beta
     // Phase I: r = K xp - rhs, yv = M^-1 r, p = -yv, rTy, ||r||
     T* pA = sc->p_parity ? pr.p1 : pr.p0;
+    // blk (block-Jacobi): M^-1 r needs the whole block of r, so it is a
+    // second pass after a group barrier (one more barrier per iteration)
     Acc<T> sm1[1];
     T mx1[1] = {T(0)};
     kkt_rows(g, kktL, pr.P, pr.At, [&](int c) { return xp[c]; }, [&](int c) { return m ? pr.t[c] : T(0); },
       [&](int i, T pv, T av) {
         const T kx = sig * xp[i] + pv + av;
         const T r = kx - pr.rhs[i];
-        const T yv = pr.Minv[i] * r;
-        pr.r[i] = r; pr.yv[i] = yv; g.put(pA, i, -yv);
-        sm1[0].add_prod(yv, r);
+        pr.r[i] = r;
         mx1[0] = tmax(mx1[0], (T)fabs(r));
+        if (!blk) {
+          const T yv = pr.Minv[i] * r;
+          pr.yv[i] = yv; g.put(pA, i, -yv);
+          sm1[0].add_prod(yv, r);
+        }
       });
+    if (blk) {
+      if (!g.sync()) return -1;
+      for_n(g, n, [&](int i) {
+        const T yv = block_apply(pr.Binv, pr.r, n, i);
+        pr.yv[i] = yv; g.put(pA, i, -yv);
+        sm1[0].add_prod(yv, pr.r[i]);
+      });
+    }
     double rs1[1], rm1[1];
     // bd[0] = rTy, bi[0] = continue, bi[1] = iterations
     g.reduce(sm1, mx1, rs1, rm1, [&](const double* rsum, const double* rmax) {
@@ -628,11 +815,21 @@ struct Solver {
         g.put(xp, i, xp[i] + at * p[i]);
         const T r = pr.r[i] + at * pr.Kp[i];
         pr.r[i] = r;
-        const T yv = pr.Minv[i] * r;
-        pr.yv[i] = yv;
-        sm3[0].add_prod(yv, r);
         mx3[0] = tmax(mx3[0], (T)fabs(r));
+        if (!blk) {
+          const T yv = pr.Minv[i] * r;
+          pr.yv[i] = yv;
+          sm3[0].add_prod(yv, r);
+        }
       });
+      if (blk) {
+        if (!g.sync()) return -1;
+        for_n(g, n, [&](int i) {
+          const T yv = block_apply(pr.Binv, pr.r, n, i);
+          pr.yv[i] = yv;
+          sm3[0].add_prod(yv, pr.r[i]);
+        });
+      }
       double rs3[1], rm3[1];
       g.reduce(sm3, mx3, rs3, rm3, [&](const double* rsum, const double* rmax) {
         const double rTy_new = rsum[0];

@@ -13,6 +13,9 @@ generic CSR; every vector operand counted once per use (ideal reuse).
                + B_pcg [the PCG start-up product r = K x - rhs]
   residual / termination evaluation (every check_termination iterations):
       B_term = B(P_full) + B(A) + B(A') + 8*(n + m)*w
+  block-Jacobi preconditioner (cg_precond = 2): the PCG iteration reads the
+      32 x 32 blocks of M^-1, ceil(n / 32) * 1024 * w bytes, instead of the
+      n*w diagonal
 """
 from __future__ import annotations
 
@@ -21,18 +24,20 @@ def spmv_bytes(rows: int, cols: int, nnz: int, w: int) -> int:
     return nnz * (w + 4) + (rows + 1) * 4 + cols * w + rows * w
 
 
-def qp_bytes(n: int, m: int, nnz_pfull: int, nnz_a: int, w: int):
+def qp_bytes(n: int, m: int, nnz_pfull: int, nnz_a: int, w: int, block_precond: bool = False):
     bp = spmv_bytes(n, n, nnz_pfull, w)
     ba = spmv_bytes(m, n, nnz_a, w)
     bat = spmv_bytes(n, m, nnz_a, w)
     pcg = bp + ba + bat + m * w + 9 * n * w
+    if block_precond:
+        pcg += ((n + 31) // 32) * 1024 * w - n * w
     admm = bat + ba + 10 * n * w + 12 * m * w + pcg
     term = bp + ba + bat + 8 * (n + m) * w
     return pcg, admm, term
 
 
-def solve_bytes(n, m, nnz_pfull, nnz_a, w, admm_iters, pcg_iters, check_termination):
-    pcg, admm, term = qp_bytes(n, m, nnz_pfull, nnz_a, w)
+def solve_bytes(n, m, nnz_pfull, nnz_a, w, admm_iters, pcg_iters, check_termination, block_precond=False):
+    pcg, admm, term = qp_bytes(n, m, nnz_pfull, nnz_a, w, block_precond)
     checks = admm_iters // max(1, check_termination) + 1
     return pcg_iters * pcg + admm_iters * admm + checks * term
 

@@ -34,18 +34,19 @@ def optimum(oracle_lib, d):
     return r.info["status_val"], r.info["obj_val"]
 
 
-def check_against_oracles(oracle_lib, d, status, obj_gpu, prec):
+def check_against_oracles(oracle_lib, d, status, obj_gpu, prec, settings=WORKLOAD):
     """Status of the reference's builtin (direct) algebra; trajectory of the
-    same-algorithm FP64 oracle (indirect); objective error against the true
-    optimum no worse than 3x the direct oracle's own at the same eps, or eps."""
+    same-algorithm FP64 oracle (indirect, same preconditioner); objective
+    error against the true optimum no worse than 3x the direct oracle's own at
+    the same eps, or eps."""
     sd = OSQP(oracle_lib)
-    assert sd.setup(*d, linsys_solver=DIRECT_SOLVER, **WORKLOAD) == 0
+    assert sd.setup(*d, linsys_solver=DIRECT_SOLVER, **settings) == 0
     rd = sd.solve()
     assert status == rd.info["status_val"]
     if status != SOLVED:
         return
     si = OSQP(oracle_lib)
-    assert si.setup(*d, linsys_solver=INDIRECT_SOLVER, **WORKLOAD) == 0
+    assert si.setup(*d, linsys_solver=INDIRECT_SOLVER, **settings) == 0
     ri = si.solve()
     st_opt, opt = optimum(oracle_lib, d)
     assert st_opt == SOLVED

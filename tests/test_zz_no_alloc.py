@@ -28,7 +28,8 @@ def _bind(alg):
 
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("vector_rho", [True, False])
-def test_noalloc_matches_linsys_solver(prec, vector_rho):
+@pytest.mark.parametrize("precond", [1, 2])   # diagonal, block-Jacobi
+def test_noalloc_matches_linsys_solver(prec, vector_rho, precond):
     from osqp_gb300.algebra import AlgebraLib
     alg = AlgebraLib(prec)
     noalloc = _bind(alg)
@@ -40,6 +41,7 @@ def test_noalloc_matches_linsys_solver(prec, vector_rho):
     MP, MA = alg.mat(P, triu=True), alg.mat(A)
     st = alg.default_settings()
     st.rho, st.sigma = 0.1, 1e-6
+    st.cg_precond = precond
     rho = alg.vec(np.where(np.arange(m) % 3 == 0, 100.0, 0.1)) if vector_rho else None
     for call in range(2):
         rhs = np.random.default_rng(100 + call).standard_normal(n + m)
