@@ -132,6 +132,10 @@ OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** s, const OSQPMatrix* P, c
                                         const OSQPVectorf* rho_vec, const OSQPSettings* settings,
                                         OSQPFloat* scaled_prim_res, OSQPFloat* scaled_dual_res,
                                         OSQPInt polishing);                                   /* :46 */
+/* settings->cg_precond: 0 none, 1 diagonal (as the reference's CUDA PCG,
+ * cuda_pcg_interface.cu:133), 2 the 32 x 32 block-Jacobi preconditioner of
+ * this library (blocks of P + sigma I + A' R A, rebuilt by update_rho_vec and
+ * update_matrices; also selectable later through update_settings). */
 
 /* One reduced-KKT solve that allocates nothing (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc where they solve --
@@ -142,8 +146,10 @@ OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** s, const OSQPMatrix* P, c
  * (length n + m), exactly as a freshly initialised LinSysSolver's
  * solve(b, 1) does.  Its work vectors live in a fixed 4 MiB device array
  * inside the library (each GPU that loads the library holds it until the
- * process exits), so 8 n-vectors plus one m-vector, each rounded up to 256
- * bytes, must fit in 4 MiB; larger problems return
+ * process exits), so 8 n-vectors plus one m-vector (plus, with
+ * settings->cg_precond = 2, the ceil(n / 32) * 1024 values of the
+ * block-Jacobi blocks), each rounded up to 256 bytes, must fit in 4 MiB;
+ * larger problems return
  * OSQP_DATA_VALIDATION_ERROR.  The first call on a device looks up that
  * array's device address; make it before any stream capture begins.  All
  * calls share the one array: calls that overlap on the GPU (other threads,
