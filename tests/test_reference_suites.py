@@ -1,0 +1,72 @@
+"""Reference suites restated against the FP64 oracle (CPU): the four cases of
+tests/primal_dual_infeasibility/test_primal_dual_infeasibility.cpp and the
+non-convex detection of tests/non_cvx/test_non_cvx.cpp, on the generators'
+data (tests/golden/ref_tests.npz).  The GPU runs the same cases in
+test_reference_suites_gpu.py."""
+import numpy as np
+import pytest
+
+from osqp_gb300 import problems as pb
+from osqp_gb300.api import (OSQP, SOLVED, PRIMAL_INFEASIBLE, DUAL_INFEASIBLE, NON_CVX, MAX_ITER_REACHED,
+                            DIRECT_SOLVER, INDIRECT_SOLVER)
+from conftest import csc_from, problem_from
+
+# OSQPTestFixture settings (tests/osqp_tester.h:60-80)
+FIXTURE = dict(rho=0.1, alpha=1.6, max_iter=2000, scaling=1, eps_abs=1e-5, eps_rel=1e-5)
+TESTS_TOL = 1e-4          # FP64 (tests/osqp_tester.h:12-16)
+NONCVX_ERROR = 4          # OSQP_NONCVX_ERROR (osqp_api_constants.h, osqp_error_type)
+PDI = "primal_dual_infeasibility/data/"
+# case -> (A, u, polishing, expected statuses) (test_primal_dual_infeasibility.cpp:11-135)
+PDI_CASES = {1: ("A12", "u1", 1, (SOLVED,)), 2: ("A12", "u2", 0, (PRIMAL_INFEASIBLE,)),
+             3: ("A34", "u3", 0, (DUAL_INFEASIBLE,)), 4: ("A34", "u4", 0, (PRIMAL_INFEASIBLE, DUAL_INFEASIBLE))}
+
+
+def pdi_problem(ref_tests, case):
+    a, u, polish, expect = PDI_CASES[case]
+    data = (csc_from(ref_tests, PDI + "P"), np.asarray(ref_tests[PDI + "q"]), csc_from(ref_tests, PDI + a),
+            np.asarray(ref_tests[PDI + "l"]), np.asarray(ref_tests[PDI + u]))
+    return data, polish, expect
+
+
+def solve(lib, data, inf, **st):
+    P, q, A, l, u = data
+    s = OSQP(lib)
+    rc = s.setup(P, q, A, pb.clip_inf(l, inf), pb.clip_inf(u, inf), **st)
+    return rc, (s.solve() if rc == 0 else None)
+
+
+@pytest.mark.parametrize("lin", [DIRECT_SOLVER, INDIRECT_SOLVER])
+@pytest.mark.parametrize("case", [1, 2, 3, 4])
+def test_primal_dual_infeasibility(oracle_lib, ref_tests, lin, case):
+    data, polish, expect = pdi_problem(ref_tests, case)
+    rc, r = solve(oracle_lib, data, 1e30, linsys_solver=lin, **dict(FIXTURE, polishing=polish, scaling=0))
+    assert rc == 0
+    assert r.info["status_val"] in expect
+    if case == 1:
+        assert np.max(np.abs(r.x - ref_tests[PDI + "x1"])) < TESTS_TOL
+        assert np.max(np.abs(r.y - ref_tests[PDI + "y1"])) < TESTS_TOL
+        assert abs(r.info["obj_val"] - float(ref_tests[PDI + "obj_value1"])) < TESTS_TOL
+
+
+def test_nonconvex_setup_detection(oracle_lib, ref_tests):
+    """Direct solver: (P + sigma I) with a negative eigenvalue fails at set-up;
+    with sigma_new it does not (test_non_cvx.cpp:10-45)."""
+    data = problem_from(ref_tests, "non_cvx")
+    st = dict(FIXTURE, adaptive_rho=0, linsys_solver=DIRECT_SOLVER)
+    rc, _ = solve(oracle_lib, data, 1e30, **dict(st, sigma=1e-6))
+    assert rc == NONCVX_ERROR
+    rc, _ = solve(oracle_lib, data, 1e30, **dict(st, sigma=float(ref_tests["non_cvx/sols/sigma_new"])))
+    assert rc == 0
+
+
+def test_nonconvex_solve(oracle_lib, ref_tests):
+    """Solve with sigma_new: status non-convex, objective NaN (test_non_cvx.cpp:48-78).
+    The same PCG algorithm in FP64 diverges too, but with OSQP_INFTY = 1e30
+    its residuals (2.8e18 at 2000 iterations) stay below the divergence test."""
+    data = problem_from(ref_tests, "non_cvx")
+    st = dict(FIXTURE, adaptive_rho=0, sigma=float(ref_tests["non_cvx/sols/sigma_new"]))
+    _, rd = solve(oracle_lib, data, 1e30, linsys_solver=DIRECT_SOLVER, **st)
+    assert rd.info["status_val"] == NON_CVX and np.isnan(rd.info["obj_val"])
+    _, ri = solve(oracle_lib, data, 1e30, linsys_solver=INDIRECT_SOLVER, **st)
+    assert ri.info["status_val"] == MAX_ITER_REACHED
+    assert ri.info["prim_res"] > 1e17 and ri.info["dual_res"] > 1e17
