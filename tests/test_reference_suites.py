@@ -70,3 +70,24 @@ def test_nonconvex_solve(oracle_lib, ref_tests):
     _, ri = solve(oracle_lib, data, 1e30, linsys_solver=INDIRECT_SOLVER, **st)
     assert ri.info["status_val"] == MAX_ITER_REACHED
     assert ri.info["prim_res"] > 1e17 and ri.info["dual_res"] > 1e17
+
+
+def large_qp():
+    """tests/large_qp/large_qp_data.c (prob1, n = 160, m = 270), read as text by
+    tests/golden/make_large_qp.py."""
+    import os
+    import scipy.sparse as sp
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "large_qp.npz"))
+    n, m = int(d["n"]), int(d["m"])
+    P = sp.csc_matrix((d["P_csc_x"], d["P_csc_i"], d["P_csc_p"]), shape=(n, n))
+    A = sp.csc_matrix((d["A_csc_x"], d["A_csc_i"], d["A_csc_p"]), shape=(m, n))
+    return (P, d["q_val"], A, d["l_val"], d["u_val"]), float(d["obj_val"])
+
+
+@pytest.mark.parametrize("lin", [DIRECT_SOLVER, INDIRECT_SOLVER])
+def test_large_qp(oracle_lib, lin):
+    """Solved, objective within TESTS_TOL relative of 0.106081 (test_large_qp.cpp:10-37)."""
+    data, obj = large_qp()
+    rc, r = solve(oracle_lib, data, 1e30, linsys_solver=lin, **FIXTURE)
+    assert rc == 0 and r.info["status_val"] == SOLVED
+    assert abs(r.info["obj_val"] - obj) / abs(obj) < TESTS_TOL

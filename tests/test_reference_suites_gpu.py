@@ -157,3 +157,13 @@ def test_batch_device_pointers_match_host_arrays():
     assert dev.solution_ptr(x_ptr=x_dev.data_ptr()) == 0
     assert np.array_equal(x_dev.cpu().numpy(), x_host)
     host.cleanup(); dev.cleanup()
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_large_qp(prec):
+    """Solved, objective within TESTS_TOL relative of 0.106081 (test_large_qp.cpp:10-37)."""
+    from test_reference_suites import large_qp
+    data, obj = large_qp()
+    rc, r = solve(load(prec), data, INF[prec], **FIXTURE)
+    assert rc == 0 and r.info["status_val"] == SOLVED
+    assert abs(r.info["obj_val"] - obj) / abs(obj) < TESTS_TOL[prec]
