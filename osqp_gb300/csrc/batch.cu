@@ -877,8 +877,8 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   BT_TRY(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice, s));
   b->order_h = order;
   b->work_h.assign(work.begin(), work.end());
-  BT_TRY(cudaMemcpyAsync(B.Praw, Px, sizeof(T) * pto, cudaMemcpyDefault, s));
-  BT_TRY(cudaMemcpyAsync(B.Araw, Ax, sizeof(T) * ao, cudaMemcpyDefault, s));
+  if (pto) BT_TRY(cudaMemcpyAsync(B.Praw, Px, sizeof(T) * pto, cudaMemcpyDefault, s));
+  if (ao) BT_TRY(cudaMemcpyAsync(B.Araw, Ax, sizeof(T) * ao, cudaMemcpyDefault, s));
   BT_TRY(cudaMemcpyAsync(B.vn[1], q, sizeof(T) * nsum, cudaMemcpyDefault, s));
   if (msum) {
     BT_TRY(cudaMemcpyAsync(B.vm[2], l, sizeof(T) * msum, cudaMemcpyDefault, s));

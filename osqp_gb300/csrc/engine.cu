@@ -405,13 +405,18 @@ OSQPCscMatrix* OSQPCscMatrix_new(OSQPInt m, OSQPInt n, OSQPInt nzmax, OSQPFloat*
 void OSQPCscMatrix_set_data(OSQPCscMatrix* M, OSQPInt m, OSQPInt n, OSQPInt nzmax, OSQPFloat* x, OSQPInt* i, OSQPInt* p) {
   M->m = m; M->n = n; M->nzmax = nzmax; M->nz = -1; M->x = x; M->i = i; M->p = p; M->owned = 0;
 }
+// An owned m x n matrix with room for nnz entries; a matrix without entries
+// has NULL i and x (src/osqp_api.c:122-145).
 static OSQPCscMatrix* csc_owned(OSQPInt m, OSQPInt n, OSQPInt nnz) {
   OSQPCscMatrix* M = (OSQPCscMatrix*)calloc(1, sizeof(OSQPCscMatrix));
   if (!M) return NULL;
   M->m = m; M->n = n; M->nzmax = nnz; M->nz = -1; M->owned = 1;
   M->p = (OSQPInt*)calloc((size_t)n + 1, sizeof(OSQPInt));
-  M->i = (OSQPInt*)calloc((size_t)(nnz > 0 ? nnz : 1), sizeof(OSQPInt));
-  M->x = (OSQPFloat*)calloc((size_t)(nnz > 0 ? nnz : 1), sizeof(OSQPFloat));
+  if (nnz > 0) {
+    M->i = (OSQPInt*)calloc((size_t)nnz, sizeof(OSQPInt));
+    M->x = (OSQPFloat*)calloc((size_t)nnz, sizeof(OSQPFloat));
+  }
+  if (!M->p || (nnz > 0 && (!M->i || !M->x))) { OSQPCscMatrix_free(M); return NULL; }
   return M;
 }
 void OSQPCscMatrix_free(OSQPCscMatrix* M) {
@@ -634,8 +639,8 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
 
   // ---- raw data in (host or device pointers) ----
   cudaStream_t s = w->stream;
-  GB_TRY(cudaMemcpyAsync((void*)pr.Praw, P->x, sizeof(T) * nnzT, cudaMemcpyDefault, s));
-  GB_TRY(cudaMemcpyAsync((void*)pr.Araw, A->x, sizeof(T) * nnzA, cudaMemcpyDefault, s));
+  if (nnzT) GB_TRY(cudaMemcpyAsync((void*)pr.Praw, P->x, sizeof(T) * nnzT, cudaMemcpyDefault, s));
+  if (nnzA) GB_TRY(cudaMemcpyAsync((void*)pr.Araw, A->x, sizeof(T) * nnzA, cudaMemcpyDefault, s));
   GB_TRY(cudaMemcpyAsync((void*)pr.q_in, q, sizeof(T) * n, cudaMemcpyDefault, s));
   if (m) {
     GB_TRY(cudaMemcpyAsync((void*)pr.l_in, l, sizeof(T) * m, cudaMemcpyDefault, s));
