@@ -91,3 +91,57 @@ def test_large_qp(oracle_lib, lin):
     rc, r = solve(oracle_lib, data, 1e30, linsys_solver=lin, **FIXTURE)
     assert rc == 0 and r.info["status_val"] == SOLVED
     assert abs(r.info["obj_val"] - obj) / abs(obj) < TESTS_TOL
+
+
+UPD = "update_matrices/data/test_solve_"
+# section -> (update P, update A, index vectors, counts of 0 = "all", expected answers)
+# (tests/update_matrices/test_update_matrices.cpp:94-383)
+UPDATE_SECTIONS = {
+    "P_idx": (True, False, True, False, "P_new"), "P_all": (True, False, False, False, "P_new"),
+    "P_nnz0": (True, False, False, True, "P_new"), "A_idx": (False, True, True, False, "A_new"),
+    "A_all": (False, True, False, False, "A_new"), "A_nnz0": (False, True, False, True, "A_new"),
+    "PA_idx": (True, True, True, False, "P_A_new"), "PA_all": (True, True, False, False, "P_A_new"),
+    "PA_nnz0": (True, True, False, True, "P_A_new"),
+}
+
+
+def update_matrices(s, Px, Px_idx, pn, Ax, Ax_idx, an):
+    """osqp_update_data_mat with explicit counts (0 with values = all entries)."""
+    import ctypes as C
+    L = s.L
+    arr = lambda a, dt, T: None if a is None else np.ascontiguousarray(a, dtype=dt).ctypes.data_as(C.POINTER(T))
+    keep = [None if a is None else np.ascontiguousarray(a) for a in (Px, Px_idx, Ax, Ax_idx)]
+    rc = L.lib.osqp_update_data_mat(s._solver, arr(Px, L.np_float, L.F), arr(Px_idx, np.int32, L.I), pn,
+                                    arr(Ax, L.np_float, L.F), arr(Ax_idx, np.int32, L.I), an)
+    del keep
+    return int(rc)
+
+
+def run_update_section(lib, ref_tests, section, inf, tol, **extra):
+    upd_p, upd_a, with_idx, zero, ans = UPDATE_SECTIONS[section]
+    Pu, A = csc_from(ref_tests, UPD + "Pu"), csc_from(ref_tests, UPD + "A")
+    q, l, u = (np.asarray(ref_tests[UPD + k]) for k in ("q", "l", "u"))
+    s = OSQP(lib)
+    assert s.setup(Pu, q, A, pb.clip_inf(l, inf), pb.clip_inf(u, inf), **dict(FIXTURE, max_iter=1000, **extra)) == 0
+    r = s.solve()
+    assert r.info["status_val"] == SOLVED
+    assert np.max(np.abs(r.x - ref_tests[UPD + "x"])) < tol
+    assert np.max(np.abs(r.y - ref_tests[UPD + "y"])) < tol
+    Pn, An = csc_from(ref_tests, UPD + "Pu_new"), csc_from(ref_tests, UPD + "A_new")
+    nP, nA = Pn.nnz, A.nnz
+    args = [None, None, 0, None, None, 0]
+    if upd_p:
+        args[0:3] = [Pn.data, np.arange(nP) if with_idx else None, 0 if zero else nP]
+    if upd_a:
+        args[3:6] = [An.data, np.arange(nA) if with_idx else None, 0 if zero else nA]
+    assert update_matrices(s, *args) == 0
+    r = s.solve()
+    assert r.info["status_val"] == SOLVED
+    assert np.max(np.abs(r.x - ref_tests[UPD + ans + "_x"])) < tol
+    assert np.max(np.abs(r.y - ref_tests[UPD + ans + "_y"])) < tol
+
+
+@pytest.mark.parametrize("lin", [DIRECT_SOLVER, INDIRECT_SOLVER])
+@pytest.mark.parametrize("section", sorted(UPDATE_SECTIONS))
+def test_update_matrices(oracle_lib, ref_tests, lin, section):
+    run_update_section(oracle_lib, ref_tests, section, 1e30, TESTS_TOL, linsys_solver=lin)
