@@ -135,7 +135,9 @@ OSQPInt osqp_gb300_server_submit(OSQPServer* server, OSQPInt pool_id, OSQPInt qp
 
 /* Wait for a ticket; copies x (QP-sized, host memory, may be NULL), status,
  * iterations, objective and the request's latency in ms (submission to
- * results on the host).  Each ticket can be waited for once. */
+ * results on the host).  Each ticket can be waited for once.  Returns 0, or
+ * OSQP_ALGEBRA_LOAD_ERROR once a launch of the server has failed: from then
+ * on every waiting and later request completes with status OSQP_UNSOLVED. */
 OSQPInt osqp_gb300_server_wait(OSQPServer* server, long long ticket, OSQPFloat* x, OSQPInt* status,
                                OSQPInt* iter, OSQPFloat* obj_val, double* latency_ms);
 

@@ -1344,6 +1344,14 @@ static void serve_worker(OSQPServer* S) {
       slot_finish(S, sl);
       S->cv_done.notify_all();
     }
+    if (S->err && !S->pending.empty()) {
+      // after a failed launch no new launch is issued: every waiting request
+      // completes unsolved (its wait returns the error) instead of waiting forever
+      const double t = now_s();
+      for (ServeReq* r : S->pending) { r->done = true; r->status = OSQP_UNSOLVED; r->t1 = t; }
+      S->pending.clear();
+      S->cv_done.notify_all();
+    }
     // every free stream takes the waiting requests of the pool of the oldest
     // one (one request per QP in flight; later ones for a busy QP wait)
     for (Slot& sl : S->slots) {
@@ -1374,7 +1382,7 @@ static void serve_worker(OSQPServer* S) {
       if (take.empty()) break;
       if (slot_start(S, sl, pool, take)) {
         S->err = OSQP_ALGEBRA_LOAD_ERROR;
-        for (ServeReq* r : take) { r->done = true; r->status = OSQP_UNSOLVED; }
+        for (ServeReq* r : take) { r->done = true; r->status = OSQP_UNSOLVED; r->t1 = now_s(); }
         S->cv_done.notify_all();
         continue;
       }
@@ -1463,8 +1471,8 @@ extern "C" OSQPInt osqp_gb300_server_wait(OSQPServer* S, long long ticket, OSQPF
   ServeReq* r = it->second;
   S->cv_done.wait(lk, [&] { return r->done; });
   S->reqs.erase(it);
-  lk.unlock();
   const int err = S->err;
+  lk.unlock();
   if (x && !r->x.empty()) memcpy(x, r->x.data(), sizeof(T) * r->x.size());
   if (status) *status = r->status;
   if (iter) *iter = r->iter;
