@@ -27,3 +27,11 @@ def test_pfull_nnz_counts_the_explicit_diagonal():
     P = sp.triu(sp.csc_matrix(np.array([[2.0, 1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 3.0]])), format="csc")
     # stored triangle: (0,0) (0,1) (2,2); full with explicit diagonal: 2*3 - 2*2 + 3 = 5
     assert pfull_nnz(P) == 5
+
+
+def test_block_precond_reads_the_blocks_instead_of_the_diagonal():
+    # n = 100 -> 4 blocks of 32 x 32 values replace the 100-value diagonal per PCG iteration
+    pcg, admm, term = qp_bytes(100, 200, 400, 300, 4)
+    pcg_b, admm_b, term_b = qp_bytes(100, 200, 400, 300, 4, block_precond=True)
+    assert pcg_b - pcg == 4 * 1024 * 4 - 100 * 4
+    assert admm_b - admm == pcg_b - pcg and term_b == term
