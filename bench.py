@@ -44,6 +44,7 @@ import os
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -102,7 +103,9 @@ class ClockSampler:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", "bench_clocks.csv")
+        # the raw samples (one CSV line per 200 ms); the JSON line carries the summary
+        self.path = os.environ.get("OSQP_GB300_CLOCKS_CSV",
+                                   os.path.join(tempfile.gettempdir(), "osqp_gb300_bench_clocks.csv"))
 
     def start(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
