@@ -551,7 +551,7 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   solver->work = w;
   solver->info = (OSQPInfo*)calloc(1, sizeof(OSQPInfo));
   solver->settings = (OSQPSettings*)malloc(sizeof(OSQPSettings));
-  if (!solver->info || !solver->settings) { osqp_cleanup(solver); return OSQP_MEM_ALLOC_ERROR; }
+  if (!solver->info || !solver->settings) { osqp_cleanup(solver); *solverp = NULL; return OSQP_MEM_ALLOC_ERROR; }
   memcpy(solver->settings, settings, sizeof(OSQPSettings));
   *solverp = solver;
 
@@ -563,8 +563,8 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   w->nnzPf = 2 * w->nnzT - ndiag + (n - ndiag);
   const int nnzT = w->nnzT, nnzA = w->nnzA, nnzPf = w->nnzPf;
 
-  if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) { osqp_cleanup(solver); return OSQP_ALGEBRA_LOAD_ERROR; }
-  if (cudaEventCreate(&w->ev0) != cudaSuccess || cudaEventCreate(&w->ev1) != cudaSuccess) { osqp_cleanup(solver); return OSQP_ALGEBRA_LOAD_ERROR; }
+  if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_ALGEBRA_LOAD_ERROR; }
+  if (cudaEventCreate(&w->ev0) != cudaSuccess || cudaEventCreate(&w->ev1) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_ALGEBRA_LOAD_ERROR; }
 
   // Execution form: one CTA for small problems, cooperative grid otherwise.
   // Execution form by problem size: one CTA, one thread-block cluster, or
@@ -609,7 +609,7 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   const int gb = w->use_grid ? w->grid_blocks : 1;
   size_t o_part = ap.take<double>((size_t)(4 * kMaxSum + 2 * kMaxMax) * gb);
   w->arena_bytes = ap.off;
-  if (cudaMalloc(&w->arena, w->arena_bytes) != cudaSuccess) { osqp_cleanup(solver); return OSQP_MEM_ALLOC_ERROR; }
+  if (cudaMalloc(&w->arena, w->arena_bytes) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_MEM_ALLOC_ERROR; }
   cudaMemsetAsync(w->arena, 0, w->arena_bytes, w->stream);
   char* b = w->arena;
   DevProblem<T>& pr = w->pr;
@@ -709,9 +709,9 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   if (st->adaptive_rho == OSQP_ADAPTIVE_RHO_UPDATE_KKT_ERROR && st->adaptive_rho_interval == 0)
     st->adaptive_rho_interval = 1;
   w->ds = make_dev_settings(st);
-  if (ensure_block_precond(w)) { osqp_cleanup(solver); return OSQP_MEM_ALLOC_ERROR; }
+  if (ensure_block_precond(w)) { osqp_cleanup(solver); *solverp = NULL; return OSQP_MEM_ALLOC_ERROR; }
 
-  if (cudaMallocHost((void**)&w->h_st, sizeof(SolverScalars)) != cudaSuccess) { osqp_cleanup(solver); return OSQP_MEM_ALLOC_ERROR; }
+  if (cudaMallocHost((void**)&w->h_st, sizeof(SolverScalars)) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_MEM_ALLOC_ERROR; }
   int rc = launch_setup(w, 0);
   if (rc) { osqp_cleanup(solver); *solverp = NULL; return rc; }
 
