@@ -345,6 +345,8 @@ class Batch:
         L.osqp_gb300_batch_cleanup.restype = I
         L.osqp_gb300_batch_autotune.argtypes = [C.c_void_p, I, C.POINTER(I)]
         L.osqp_gb300_batch_autotune.restype = I
+        L.osqp_gb300_batch_qp_seconds.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.osqp_gb300_batch_qp_seconds.restype = I
 
     @staticmethod
     def pack(problems, float_dtype):
@@ -435,7 +437,6 @@ class Batch:
     def qp_seconds(self):
         """Device time of every QP's last solve (seconds)."""
         out = np.zeros(self.count, np.float64)
-        self.L.lib.osqp_gb300_batch_qp_seconds.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         self.L.lib.osqp_gb300_batch_qp_seconds(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
