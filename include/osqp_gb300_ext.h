@@ -22,6 +22,14 @@ extern "C" {
 OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter, long long* pcg_iter,
                                double* kernel_ms, OSQPInt* grid_form);
 
+/* Interrupt the solve running on `solver` (from another thread): the solve
+ * stops at its next ADMM iteration with status OSQP_SIGINT, stores no
+ * solution and osqp_solve returns 1, as after Ctrl-C (osqp_api.c:728-737).
+ * osqp_solve itself turns a SIGINT that arrives while it runs into the same
+ * request; the previous SIGINT handler is restored when it returns.  A request
+ * counts for the solve in progress only.  Returns 0 on success. */
+OSQPInt osqp_gb300_interrupt(OSQPSolver* solver);
+
 /* ---- Block-Jacobi preconditioner -------------------------------------------
  * settings->cg_precond = OSQP_GB300_BLOCK_DIAGONAL_PRECONDITIONER (an
  * extension of osqp_precond_type, include/public/osqp_api_constants.h:66-69,

@@ -215,9 +215,17 @@ class OSQP:
     def solve(self) -> Result:
         L = self.L
         rc = L.lib.osqp_solve(self._solver)
-        if rc not in (0,):
+        # 1 with status "interrupted": the solve was interrupted (Ctrl-C or interrupt())
+        if rc != 0 and not (rc == 1 and self._solver.contents.info.contents.status_val == SIGINT):
             raise RuntimeError(f"osqp_solve returned {rc}")
         return self.result()
+
+    def interrupt(self) -> int:
+        """Stop the solve running on this solver (call from another thread)."""
+        f = self.L.lib.osqp_gb300_interrupt
+        f.argtypes = [C.POINTER(self.L.Solver)]
+        f.restype = self.L.I
+        return int(f(self._solver))
 
     def result(self) -> Result:
         s = self._solver.contents

@@ -18,7 +18,11 @@
 #include <string.h>
 #include <time.h>
 
+#include <signal.h>
+
 #include <algorithm>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "osqp_gb300.h"
@@ -255,6 +259,56 @@ struct OSQPWorkspace_ {
   cudaEvent_t ev0, ev1;
   float last_kernel_ms;
   void* polish;           // polish workspace (gb_polish.cu)
+  cudaStream_t cancel_stream;  // interrupt requests: a write of pr.st->cancel beside the running solve
+  int* h_one;                  // pinned 1, the value that write copies
+};
+
+// Interrupt of a running solve (osqp_api.c:728-737, interrupt_unix.c): the
+// solve kernel reads pr.st->cancel once per ADMM iteration (it rides on the
+// iteration's first reduction, so every CTA stops at the same iteration) and
+// ends with status OSQP_SIGINT.  The request is a copy into that word on a
+// stream of its own, which runs while the solve kernel does.
+static int request_cancel(OSQPWorkspace* w) {
+  if (cudaSetDevice(w->device) != cudaSuccess) return OSQP_ALGEBRA_LOAD_ERROR;
+  if (cudaMemcpyAsync(&w->pr.st->cancel, w->h_one, sizeof(int), cudaMemcpyHostToDevice, w->cancel_stream) != cudaSuccess ||
+      cudaStreamSynchronize(w->cancel_stream) != cudaSuccess)
+    return OSQP_ALGEBRA_LOAD_ERROR;
+  return 0;
+}
+
+// Ctrl-C during osqp_solve, as the reference's listener: a SIGINT handler is
+// installed while solves run and the previous one restored after.  Solves
+// running at the same time (other threads) share one installation, counted,
+// so the caller's handler comes back when the last of them returns.  The
+// handler only bumps a counter; each thread waiting for a solve turns a
+// change of it into an interrupt request for its own solve.
+static volatile sig_atomic_t g_sigint = 0;
+static void on_sigint(int) { g_sigint = g_sigint + 1; }
+static std::mutex g_listener_mu;
+static int g_listeners = 0;
+static struct sigaction g_saved_act;
+static bool g_installed = false;
+struct InterruptListener {
+  sig_atomic_t seen;
+  InterruptListener() {
+    std::lock_guard<std::mutex> lk(g_listener_mu);
+    if (g_listeners++ == 0) {
+      struct sigaction act;
+      memset(&act, 0, sizeof(act));
+      act.sa_handler = on_sigint;
+      sigemptyset(&act.sa_mask);
+      g_installed = sigaction(SIGINT, &act, &g_saved_act) == 0;
+    }
+    seen = g_sigint;
+  }
+  bool fired() const { return g_sigint != seen; }
+  ~InterruptListener() {
+    std::lock_guard<std::mutex> lk(g_listener_mu);
+    if (--g_listeners == 0 && g_installed) {
+      sigaction(SIGINT, &g_saved_act, nullptr);
+      g_installed = false;
+    }
+  }
 };
 
 // Block-Jacobi storage, allocated when cg_precond = 2 is first asked for
@@ -523,6 +577,8 @@ static void free_workspace(OSQPWorkspace* w) {
   if (w->polish) { gb_polish_free(w->polish); w->polish = NULL; }
   if (w->arena) cudaFree(w->arena);
   if (w->pr.Binv) cudaFree(w->pr.Binv);
+  if (w->cancel_stream) cudaStreamDestroy(w->cancel_stream);
+  if (w->h_one) cudaFreeHost(w->h_one);
   if (w->h_x) cudaFreeHost(w->h_x);
   if (w->h_st) cudaFreeHost(w->h_st);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -563,7 +619,12 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   w->nnzPf = 2 * w->nnzT - ndiag + (n - ndiag);
   const int nnzT = w->nnzT, nnzA = w->nnzA, nnzPf = w->nnzPf;
 
-  if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_ALGEBRA_LOAD_ERROR; }
+  if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&w->cancel_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMallocHost((void**)&w->h_one, sizeof(int)) != cudaSuccess) {
+    osqp_cleanup(solver); *solverp = NULL; return OSQP_ALGEBRA_LOAD_ERROR;
+  }
+  *w->h_one = 1;
   if (cudaEventCreate(&w->ev0) != cudaSuccess || cudaEventCreate(&w->ev1) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_ALGEBRA_LOAD_ERROR; }
 
   // Execution form: one CTA for small problems, cooperative grid otherwise.
@@ -775,6 +836,9 @@ static int launch_setup(OSQPWorkspace* w, int keep_state) {
 static int launch_solve(OSQPWorkspace* w) {
   cudaStream_t s = w->stream;
   cudaMemsetAsync(w->bar, 0, sizeof(unsigned int) * 4 + sizeof(int) * 4, s);
+  // an interrupt counts for the solve it arrives in (the reference's
+  // listener also starts clear on every solve)
+  GB_TRY(cudaMemsetAsync(&w->pr.st->cancel, 0, sizeof(int), s));
   cudaEventRecord(w->ev0, s);
   if (w->use_grid) {
     GridSync gs; grid_sync_args(w, gs);
@@ -829,9 +893,19 @@ extern "C" OSQPInt osqp_solve(OSQPSolver* solver) {
   if (w->clear_update_time) info->update_time = 0.0;
   double t0 = wall_s();
   cudaSetDevice(w->device);
-  int rc = launch_solve(w);
-  if (rc) return rc;
-  cudaMemcpyAsync(w->h_st, w->pr.st, sizeof(SolverScalars), cudaMemcpyDeviceToHost, w->stream);
+  int rc;
+  {
+    InterruptListener listener;
+    rc = launch_solve(w);
+    if (rc) return rc;
+    cudaMemcpyAsync(w->h_st, w->pr.st, sizeof(SolverScalars), cudaMemcpyDeviceToHost, w->stream);
+    // wait for the solve; a Ctrl-C meanwhile becomes an interrupt request
+    bool sent = false;
+    while (cudaStreamQuery(w->stream) == cudaErrorNotReady) {
+      if (!sent && listener.fired()) { request_cancel(w); sent = true; }
+      std::this_thread::yield();
+    }
+  }
   rc = check_device_error(w);
   if (rc) return rc;
   cudaEventElapsedTime(&w->last_kernel_ms, w->ev0, w->ev1);
@@ -848,10 +922,17 @@ extern "C" OSQPInt osqp_solve(OSQPSolver* solver) {
   info->run_time = (w->first_run ? info->setup_time : info->update_time) + info->solve_time + info->polish_time;
   w->first_run = 0;
   w->clear_update_time = 1;
+  // an interrupted solve stores no solution and returns 1 (osqp_api.c:730-736)
+  if (info->status_val == OSQP_SIGINT) return 1;
   rc = copy_solution(w, solver->solution);
   if (rc) return rc;
   if (cudaStreamSynchronize(w->stream) != cudaSuccess) return OSQP_ALGEBRA_LOAD_ERROR;
   return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_interrupt(OSQPSolver* solver) {
+  if (!solver || !solver->work) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  return request_cancel(solver->work);
 }
 
 extern "C" OSQPInt osqp_get_solution(OSQPSolver* solver, OSQPSolution* solution) {
