@@ -145,3 +145,94 @@ def run_update_section(lib, ref_tests, section, inf, tol, **extra):
 @pytest.mark.parametrize("section", sorted(UPDATE_SECTIONS))
 def test_update_matrices(oracle_lib, ref_tests, lin, section):
     run_update_section(oracle_lib, ref_tests, section, 1e30, TESTS_TOL, linsys_solver=lin)
+
+
+# ---- tests/basic_qp/test_basic_qp.cpp and tests/basic_qp2/test_basic_qp2.cpp ----
+DATA_VALIDATION_ERROR = 1   # OSQP_DATA_VALIDATION_ERROR (osqp_api_constants.h, osqp_error_type)
+
+
+def _basic(ref_tests, name="basic_qp"):
+    return problem_from(ref_tests, name)
+
+
+def _close_rel(v, ref, tol):
+    return np.max(np.abs(v - ref)) / max(np.max(np.abs(ref)), 1e-12) < tol
+
+
+@pytest.mark.parametrize("lin", [DIRECT_SOLVER, INDIRECT_SOLVER])
+def test_basic_qp_termination(oracle_lib, ref_tests, lin):
+    """check_termination = 0: the loop runs max_iter iterations and the final
+    check still finds the solution (test_basic_qp.cpp:718-775)."""
+    data = _basic(ref_tests)
+    st = dict(max_iter=400, alpha=1.6, polishing=0, scaling=0, check_termination=0, warm_starting=0)
+    rc, r = solve(oracle_lib, data, 1e30, linsys_solver=lin, **st)
+    assert rc == 0 and r.info["iter"] == 400 and r.info["status_val"] == SOLVED
+    assert np.max(np.abs(r.x - ref_tests["basic_qp/sols/x_test"])) < TESTS_TOL
+    assert np.max(np.abs(r.y - ref_tests["basic_qp/sols/y_test"])) < TESTS_TOL
+    assert abs(r.info["obj_val"] - float(ref_tests["basic_qp/sols/obj_value_test"])) < TESTS_TOL
+
+
+def test_basic_qp_update_validation(oracle_lib, ref_tests):
+    """Flipped bounds are refused and leave the problem as it was
+    (test_basic_qp.cpp:608-716)."""
+    P, q, A, l, u = _basic(ref_tests)
+    s = OSQP(oracle_lib)
+    assert s.setup(P, q, A, pb.clip_inf(l, 1e30), pb.clip_inf(u, 1e30),
+                   **dict(FIXTURE, max_iter=200, polishing=1, scaling=0, warm_starting=0)) == 0
+    u_new, l_new = ref_tests["basic_qp/sols/u_new"], ref_tests["basic_qp/sols/l_new"]
+    assert s.update(l=pb.clip_inf(u_new, 1e30), u=pb.clip_inf(l_new, 1e30)) == DATA_VALIDATION_ERROR
+    assert s.update(l=pb.clip_inf(u_new, 1e30)) == DATA_VALIDATION_ERROR
+    r = s.solve()
+    assert r.info["status_val"] == SOLVED
+    assert np.max(np.abs(r.x - ref_tests["basic_qp/sols/x_test"])) < TESTS_TOL
+
+
+@pytest.mark.parametrize("lin", [DIRECT_SOLVER, INDIRECT_SOLVER])
+def test_basic_qp_update_rho(oracle_lib, ref_tests, lin):
+    """A solver set up with rho 0.7 and one set up with 0.1 then updated to 0.7
+    take the same iterations to the same answer (test_basic_qp.cpp:776-888)."""
+    data = _basic(ref_tests)
+    st = dict(adaptive_rho=0, eps_abs=5e-5, eps_rel=5e-5, check_termination=1, linsys_solver=lin)
+    rc, r1 = solve(oracle_lib, data, 1e30, rho=0.7, **st)
+    P, q, A, l, u = data
+    s = OSQP(oracle_lib)
+    assert s.setup(P, q, A, pb.clip_inf(l, 1e30), pb.clip_inf(u, 1e30), rho=0.1, **st) == 0
+    assert s.update_rho(0.7) == 0
+    r2 = s.solve()
+    for r in (r1, r2):
+        assert r.info["status_val"] == SOLVED
+        assert _close_rel(r.x, ref_tests["basic_qp/sols/x_test"], TESTS_TOL)
+        assert _close_rel(r.y, ref_tests["basic_qp/sols/y_test"], TESTS_TOL)
+    assert r1.info["iter"] == r2.info["iter"]
+
+
+def test_basic_qp_warm_start(oracle_lib, ref_tests):
+    """Warm start from zero repeats the cold iteration count; from the
+    solution the solve takes one iteration (test_basic_qp.cpp:945-993)."""
+    P, q, A, l, u = _basic(ref_tests)
+    s = OSQP(oracle_lib)
+    assert s.setup(P, q, A, pb.clip_inf(l, 1e30), pb.clip_inf(u, 1e30),
+                   **dict(FIXTURE, check_termination=1, adaptive_rho=0)) == 0
+    it = s.solve().info["iter"]
+    assert s.warm_start(x=np.zeros(2), y=np.zeros(4)) == 0
+    assert s.solve().info["iter"] == it
+    assert s.warm_start(x=np.array([0.3, 0.7])) == 0
+    assert s.warm_start(y=np.array([-2.9, 0.0, 0.2, 0.0])) == 0
+    assert s.solve().info["iter"] == 1
+
+
+@pytest.mark.parametrize("lin", [DIRECT_SOLVER, INDIRECT_SOLVER])
+def test_basic_qp2_update_vectors(oracle_lib, ref_tests, lin):
+    """New q and u, warm-started and polished (test_basic_qp2.cpp:74-140)."""
+    P, q, A, l, u = _basic(ref_tests, "basic_qp2")
+    s = OSQP(oracle_lib)
+    assert s.setup(P, q, A, pb.clip_inf(l, 1e30), pb.clip_inf(u, 1e30), linsys_solver=lin,
+                   warm_starting=1, polishing=1) == 0
+    assert s.update(q=ref_tests["basic_qp2/sols/q_new"]) == 0
+    assert s.update(u=pb.clip_inf(ref_tests["basic_qp2/sols/u_new"], 1e30)) == 0
+    r = s.solve()
+    assert r.info["status_val"] == SOLVED and r.info["status_polish"] == 1
+    assert _close_rel(r.x, ref_tests["basic_qp2/sols/x_test_new"], TESTS_TOL)
+    assert _close_rel(r.y, ref_tests["basic_qp2/sols/y_test_new"], TESTS_TOL)
+    obj = float(ref_tests["basic_qp2/sols/obj_value_test_new"])
+    assert abs(r.info["obj_val"] - obj) / abs(obj) < TESTS_TOL
