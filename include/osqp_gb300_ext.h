@@ -60,9 +60,24 @@ OSQPInt osqp_gb300_precond_blocks(OSQPSolver* solver, OSQPFloat* out);
  *      concatenated over k; row indices Pi and values Px concatenated.
  *   A: CSC, likewise Ap / Ai / Ax.
  *   q concatenated (sum n), l and u concatenated (sum m).
- * Pointers may be host or device memory.  Settings apply to every QP
- * (linsys_solver must be OSQP_INDIRECT_SOLVER).  A batch is used by one host
- * thread at a time (the server below owns the pools it serves). */
+ * Pointers may be host or device memory.  Settings apply to every QP.
+ * linsys_solver selects the linear-system solver of every QP:
+ *   OSQP_INDIRECT_SOLVER  the reduced-KKT PCG of the reference's CUDA backend
+ *                         (algebra/cuda/lin_sys/indirect/cuda_pcg.cu:113-208);
+ *   OSQP_DIRECT_SOLVER    an exact factorisation of K = P + sigma I + A' R A,
+ *                         refreshed on every rho change, as the builtin backend
+ *                         factors its KKT matrix (algebra/_common/lin_sys/qdldl/
+ *                         qdldl_interface.c:216-530): a block-tridiagonal LDL'
+ *                         in a level-set ordering, held per QP in device memory
+ *                         and factored / applied by the QP's CTA on chip.  Set-up
+ *                         returns OSQP_LINSYS_SOLVER_INIT_ERROR when a QP's
+ *                         ordering has a block larger than the on-chip limit
+ *                         (about 100 variables: dense couplings such as a budget
+ *                         row over all assets); such QPs take the indirect solver.
+ *                         A non-positive pivot (K not positive definite) ends
+ *                         that QP with status OSQP_NON_CVX.
+ * A batch is used by one host thread at a time (the server below owns the
+ * pools it serves). */
 typedef struct OSQPBatch_ OSQPBatch;
 
 OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, const OSQPInt* n, const OSQPInt* m,
@@ -114,6 +129,18 @@ OSQPInt osqp_gb300_batch_qp_seconds(OSQPBatch* batch, double* seconds);
 OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* batch, long long* pcg_iter);
 
 OSQPInt osqp_gb300_batch_cleanup(OSQPBatch* batch);
+
+/* Ordering of the direct solver for one QP (host memory; no device work):
+ * P upper-triangular CSC (Pp, Pi), A CSC (Ap, Ai) with m rows.  On return
+ * *nblocks blocks, block_start[0..*nblocks] (n + 1 entries of room) and perm
+ * (n entries: permuted position -> variable).  In this order every entry of
+ * P + A'A lies in a diagonal block or a first off-diagonal block.  Returns 0,
+ * 1 when a block would exceed bmax_limit variables, 2 on inconsistent input.
+ * No reference counterpart: the builtin orders its KKT matrix with AMD
+ * (algebra/_common/lin_sys/qdldl/qdldl_interface.c:94-116). */
+OSQPInt osqp_gb300_kkt_plan(OSQPInt n, OSQPInt m, const OSQPInt* Pp, const OSQPInt* Pi, const OSQPInt* Ap,
+                            const OSQPInt* Ai, OSQPInt bmax_limit, OSQPInt* nblocks, OSQPInt* block_start,
+                            OSQPInt* perm);
 
 /* ---- Request serving (continuous batching) ---------------------------------
  * A server owns a worker thread and `concurrency` CUDA streams.  QPs are made

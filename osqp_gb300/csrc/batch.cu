@@ -45,6 +45,7 @@
 #include "gb_solver.cuh"
 #include "gb_structure.cuh"
 #include "gb_launch.cuh"
+#include "gb_kkt_plan.h"
 
 using T = OSQPFloat;
 using namespace gb;
@@ -69,6 +70,10 @@ struct BatchInst {
   int kktL, PL, AL, AtL;
   int Pdiag_only;       // P holds exactly its full diagonal
   int blk_off;          // first 32 x 32 block-Jacobi block of the QP (cg_precond = 2)
+  // direct KKT solve (knb == 0: the PCG): blocks, largest block, offsets of
+  // the QP's block lists, constraint lists and factor
+  int knb, kbmax, kb_off, kcr_off;
+  long long kf_off;
 };
 
 template <typename TT>
@@ -83,6 +88,9 @@ struct BatchArrays {
   SolverScalars* st;
   const BatchInst* inst;
   TT* Binv;             // block-Jacobi blocks of every QP (nullptr unless cg_precond = 2)
+  // direct KKT solve: plans and factors of every QP (gb_kkt_plan.h)
+  int *kperm, *kiperm, *kbs, *kfo, *kco, *kcr;
+  TT* kF;
 
   __device__ DevProblem<TT> problem(int k) const {
     const BatchInst b = inst[k];
@@ -107,6 +115,13 @@ struct BatchArrays {
     pr.st = st + k;
     pr.Binv = Binv ? Binv + (size_t)b.blk_off * kPrecondBlock * kPrecondBlock : nullptr;
     pr.Arow_g = pr.A.rowptr; pr.Acol_g = Acol; pr.Aval_g = Aval;
+    if (b.knb > 0) {
+      pr.kkt.nb = b.knb; pr.kkt.bmax = b.kbmax;
+      pr.kkt.bs = kbs + b.kb_off; pr.kkt.fo = kfo + b.kb_off; pr.kkt.co = kco + b.kb_off;
+      pr.kkt.cr = kcr + b.kcr_off;
+      pr.kkt.perm = kperm + o; pr.kkt.iperm = kiperm + o;
+      pr.kkt.F = kF + b.kf_off;
+    }
     return pr;
   }
 };
@@ -288,7 +303,11 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pv.st; }
   __syncthreads();
   bool staged = false;
-  if (mode == kModeSolve && dsm_bytes > 0) {
+  // direct KKT solve: the dynamic shared memory is the factorisation's and the
+  // block solve's workspace (the QP's data stay in HBM / L2)
+  const bool direct = pv.kkt.nb > 0;
+  if (direct) pv.kws = (TT*)dsm;
+  if (mode == kModeSolve && dsm_bytes > 0 && !direct) {
     if constexpr (std::is_same<G, ClusterGroup>::value) {
       // block-Jacobi needs each block of r in one CTA: n-slices start on block boundaries
       g.sp = cluster_spans(pv, B.inst[k].kktL, (int)g.rank, (int)g.size,
@@ -316,9 +335,14 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
     });
     g.sync();
     if (s.rho_is_vec) {
-      S.set_rho_vec(g);
+      // the direct factor depends on the constraint types only through the
+      // rho vector: refactor when a type changed
+      __shared__ int s_changed;
+      if (threadIdx.x == 0) s_changed = 0;
       g.sync();
-      S.update_precond(g);
+      S.set_rho_vec(g, &s_changed);
+      g.sync();
+      if (!direct || s_changed) S.update_precond(g);
     }
     if (threadIdx.x == 0) { ssc.status = ST_UNSOLVED; ssc.rho_updates = 0; }
   }
@@ -587,6 +611,7 @@ static int env_int(const char* name, int dflt) {
 
 struct OSQPBatch_ {
   int count, device;
+  int direct;             // linsys_solver = direct: every QP has a KKT plan
   long long nsum, msum, nnzT, nnzA, nnzPf;
   size_t binv_elems;    // block-Jacobi storage (0 unless cg_precond = 2)
   cudaStream_t stream;
@@ -690,7 +715,8 @@ static int launch_batch(OSQPBatch* b, int mode, const LaunchBufs& lb, cudaStream
     L.dsm_bytes = mode == kModeSolve ? b->cdsm : 0;
     BT_TRY(launch_clusters_dsm(b->cfn, grid, b->cluster, b->cthreads, (size_t)b->cdsm, st, b->B, b->ds, L));
   } else {
-    L.dsm_bytes = mode == kModeSolve ? b->dsm : 0;
+    // the direct solver factors in every mode (set-up, updates, solves)
+    L.dsm_bytes = (mode == kModeSolve || b->direct) ? b->dsm : 0;
     b->kfn<<<grid, b->threads, (size_t)L.dsm_bytes, st>>>(b->B, b->ds, L);
     BT_TRY(cudaGetLastError());
   }
@@ -737,7 +763,8 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
                                           const OSQPSettings* settings) {
   if (!batchp || count <= 0 || !n || !m || !Pp || !Ap || !q || !settings) return OSQP_DATA_VALIDATION_ERROR;
   *batchp = NULL;
-  if (settings->linsys_solver != OSQP_INDIRECT_SOLVER) return OSQP_SETTINGS_VALIDATION_ERROR;
+  if (settings->linsys_solver != OSQP_INDIRECT_SOLVER && settings->linsys_solver != OSQP_DIRECT_SOLVER)
+    return OSQP_SETTINGS_VALIDATION_ERROR;
   if (settings->alpha <= 0 || settings->alpha >= 2 || settings->rho <= 0 || settings->sigma <= 0 ||
       settings->max_iter <= 0 || settings->adaptive_rho == OSQP_ADAPTIVE_RHO_UPDATE_TIME)
     return OSQP_SETTINGS_VALIDATION_ERROR;
@@ -821,6 +848,52 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return work[a] > work[c]; });
 
+  // ---- direct KKT solve: symbolic analysis of every QP on the host ----
+  b->direct = st.linsys_solver == OSQP_DIRECT_SOLVER;
+  const int cap_kib0 = env_int("OSQP_GB300_BATCH_SMEM_KIB", -1);
+  std::vector<KktPlan> plans;
+  long long kb_tot = 0, kcr_tot = 0, kf_tot = 0;
+  if (b->direct) {
+    // the factorisation and the block solve work in the CTA's shared memory
+    int minb0 = 1;
+    cta_form(env_int("OSQP_GB300_BATCH_THREADS", 1024), &b->kfn, &b->threads, &minb0);
+    b->dsm = configure_dsm(b->kfn, b->threads, minb0, b->device, cap_kib0 < 0 ? -1L : 1024L * cap_kib0);
+    const int blim = kkt_bmax_limit(b->threads, b->dsm, (int)sizeof(T));
+    std::vector<OSQPInt> hAi(ao > 0 ? ao : 1);
+    if (ao && cudaMemcpy(hAi.data(), Ai, sizeof(OSQPInt) * ao, cudaMemcpyDefault) != cudaSuccess) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
+    plans.resize(count);
+    std::vector<int> prc(count, 0);
+    const int nthr = std::max(1, std::min((int)std::thread::hardware_concurrency(), std::min(count, 64)));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthr; t++)
+      pool.emplace_back([&, t]() {
+        for (int k = t; k < count; k += nthr) {
+          const BatchInst& I = b->inst[k];
+          prc[k] = kkt_plan_build(I.n, I.m, hPp.data() + pp_off[k], hPi.data() + I.pt_off, hAp.data() + pp_off[k],
+                                  hAi.data() + I.a_off, blim, plans[k]);
+          if (!prc[k] && kkt_ws_elems(I.n, plans[k].bmax) * (long long)sizeof(T) > b->dsm) prc[k] = 3;
+        }
+      });
+    for (auto& th : pool) th.join();
+    for (int k = 0; k < count; k++) {
+      if (prc[k]) {
+        fprintf(stderr, "osqp_gb300 batch: direct KKT solve does not apply to QP %d (n=%d, m=%d): %s\n", k,
+                b->inst[k].n, b->inst[k].m,
+                prc[k] == 1 ? "a block of its block-tridiagonal ordering exceeds the on-chip limit"
+                : prc[k] == 3 ? "its solve vectors exceed the on-chip workspace" : "inconsistent structure");
+        delete b;
+        return OSQP_LINSYS_SOLVER_INIT_ERROR;
+      }
+      BatchInst& I = b->inst[k];
+      I.knb = plans[k].nb; I.kbmax = plans[k].bmax;
+      I.kb_off = (int)kb_tot; I.kcr_off = (int)kcr_tot; I.kf_off = kf_tot;
+      kb_tot += plans[k].nb + 1; kcr_tot += (long long)plans[k].cr.size(); kf_tot += plans[k].fsize;
+    }
+    if (kb_tot > INT32_MAX || kcr_tot > INT32_MAX) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
+  } else {
+    for (int k = 0; k < count; k++) { BatchInst& I = b->inst[k]; I.knb = 0; I.kbmax = 0; I.kb_off = 0; I.kcr_off = 0; I.kf_off = 0; }
+  }
+
   // ---- arena ----
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
@@ -843,6 +916,9 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 2);
   size_t o_sq = pl.take(sizeof(T) * nsum), o_sl = pl.take(sizeof(T) * msum), o_su = pl.take(sizeof(T) * msum);
   size_t o_binv = pl.take(sizeof(T) * b->binv_elems);
+  size_t o_kperm = pl.take(sizeof(int) * (b->direct ? nsum : 0)), o_kiperm = pl.take(sizeof(int) * (b->direct ? nsum : 0));
+  size_t o_kbs = pl.take(sizeof(int) * kb_tot), o_kfo = pl.take(sizeof(int) * kb_tot), o_kco = pl.take(sizeof(int) * kb_tot);
+  size_t o_kcr = pl.take(sizeof(int) * kcr_tot), o_kF = pl.take(sizeof(T) * kf_tot);
   {
     // admission by free device memory: refuse (rather than fail part-way)
     // when the pool and the set-up scratch would not fit
@@ -866,6 +942,9 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   for (int k = 0; k < 16; k++) { B.vn[k] = (T*)(a + o_vn[k]); B.vm[k] = (T*)(a + o_vm[k]); }
   B.ctype = (int*)(a + o_ctype); B.st = (SolverScalars*)(a + o_st);
   B.Binv = b->binv_elems ? (T*)(a + o_binv) : nullptr;
+  B.kperm = (int*)(a + o_kperm); B.kiperm = (int*)(a + o_kiperm);
+  B.kbs = (int*)(a + o_kbs); B.kfo = (int*)(a + o_kfo); B.kco = (int*)(a + o_kco); B.kcr = (int*)(a + o_kcr);
+  B.kF = (T*)(a + o_kF);
   b->d_inst = (BatchInst*)(a + o_inst); B.inst = b->d_inst;
   b->d_order = (int*)(a + o_order);
   b->d_queue = (int*)(a + o_misc); b->d_flag = b->d_queue + 1;
@@ -885,6 +964,27 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     BT_TRY(cudaMemcpyAsync(B.vm[3], u, sizeof(T) * msum, cudaMemcpyDefault, s));
   }
   BT_TRY(cudaMemcpyAsync(B.Atcol, Ai, sizeof(int) * ao, cudaMemcpyDefault, s));
+  std::vector<int> kperm_h, kiperm_h, kbs_h, kfo_h, kco_h, kcr_h;
+  if (b->direct) {
+    kperm_h.reserve(nsum); kiperm_h.reserve(nsum); kbs_h.reserve(kb_tot); kfo_h.reserve(kb_tot); kco_h.reserve(kb_tot);
+    kcr_h.reserve(kcr_tot);
+    for (int k = 0; k < count; k++) {
+      const KktPlan& q = plans[k];
+      kperm_h.insert(kperm_h.end(), q.perm.begin(), q.perm.end());
+      kiperm_h.insert(kiperm_h.end(), q.iperm.begin(), q.iperm.end());
+      kbs_h.insert(kbs_h.end(), q.bs.begin(), q.bs.end());
+      kfo_h.insert(kfo_h.end(), q.fo.begin(), q.fo.end());
+      kco_h.insert(kco_h.end(), q.co.begin(), q.co.end());
+      kcr_h.insert(kcr_h.end(), q.cr.begin(), q.cr.end());
+    }
+    BT_TRY(cudaMemcpyAsync(B.kperm, kperm_h.data(), sizeof(int) * nsum, cudaMemcpyHostToDevice, s));
+    BT_TRY(cudaMemcpyAsync(B.kiperm, kiperm_h.data(), sizeof(int) * nsum, cudaMemcpyHostToDevice, s));
+    BT_TRY(cudaMemcpyAsync(B.kbs, kbs_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
+    BT_TRY(cudaMemcpyAsync(B.kfo, kfo_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
+    BT_TRY(cudaMemcpyAsync(B.kco, kco_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
+    if (kcr_tot) BT_TRY(cudaMemcpyAsync(B.kcr, kcr_h.data(), sizeof(int) * kcr_tot, cudaMemcpyHostToDevice, s));
+    plans.clear();
+  }
 
   // ---- device structure build ----
   int *dPp = nullptr, *dAp = nullptr, *dppoff = nullptr, *dPi = nullptr;
@@ -949,7 +1049,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   b->cdsm = configure_dsm(b->cfn, b->cthreads, 1, b->device, cap);
   // OSQP_GB300_BATCH_CLUSTER: 0 = one CTA per QP (k_batch), c >= 1 = clusters
   // of c CTAs per QP (k_batch_cluster, sliced rows, replicated vectors)
-  b->cluster = std::max(0, std::min(16, env_int("OSQP_GB300_BATCH_CLUSTER", 0)));
+  b->cluster = b->direct ? 0 : std::max(0, std::min(16, env_int("OSQP_GB300_BATCH_CLUSTER", 0)));
   if (b->cluster >= 1) {
     int nclusters = max_active_clusters(b->cfn, b->cluster, b->cthreads, (size_t)b->cdsm);
     if (nclusters < 1) b->cluster = 0;
@@ -967,7 +1067,8 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   // per SM: -7 %), and QPs still running after 2000 ADMM iterations continue
   // on 8-CTA clusters with the QP in shared memory (split 600: -10 %, 1000:
   // -4 %; tail clusters of 16: -12 %, of 4: -1 %).
-  b->split = std::max(0, env_int("OSQP_GB300_BATCH_SPLIT", 2000));
+  // (the direct solver runs in the CTA form only: no split)
+  b->split = b->direct ? 0 : std::max(0, env_int("OSQP_GB300_BATCH_SPLIT", 2000));
   // 0: vectors only; 1: vectors, then matrix rows; 2: matrix rows before the
   // element-wise PCG vectors
   b->stage_mat = std::max(0, std::min(2, env_int("OSQP_GB300_BATCH_STAGE_MATRIX", 1)));
@@ -985,6 +1086,19 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   if (rc) { osqp_gb300_batch_cleanup(b); return rc; }
   if (cudaStreamSynchronize(s) != cudaSuccess) { osqp_gb300_batch_cleanup(b); return OSQP_ALGEBRA_LOAD_ERROR; }
   *batchp = b;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_kkt_plan(OSQPInt n, OSQPInt m, const OSQPInt* Pp, const OSQPInt* Pi, const OSQPInt* Ap,
+                                       const OSQPInt* Ai, OSQPInt bmax_limit, OSQPInt* nblocks, OSQPInt* block_start,
+                                       OSQPInt* perm) {
+  if (n <= 0 || m < 0 || !Pp || !Ap || !nblocks || !block_start || !perm) return 2;
+  KktPlan pl;
+  const int rc = kkt_plan_build(n, m, Pp, Pi, Ap, Ai, bmax_limit, pl);
+  if (rc) return rc;
+  *nblocks = pl.nb;
+  for (int k = 0; k <= pl.nb; k++) block_start[k] = pl.bs[k];
+  for (int p = 0; p < n; p++) perm[p] = pl.perm[p];
   return 0;
 }
 

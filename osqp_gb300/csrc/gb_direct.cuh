@@ -1,0 +1,257 @@
+// gb_direct.cuh -- direct solve of the reduced KKT system on one CTA.
+//
+// linsys_solver = OSQP_DIRECT_SOLVER.  The builtin backend solves
+// [P + sigma I, A'; A, -R^-1] [x~; nu] = [sigma x - q; z - R^-1 y] by an
+// LDL' factorisation refreshed on every rho change
+// (algebra/_common/lin_sys/qdldl/qdldl_interface.c:216-530).  Here the
+// constraint block is eliminated first, K = P + sigma I + A' R A, and K is
+// factored as a block-tridiagonal LDL' (block Thomas algorithm) in the
+// ordering of gb_kkt_plan.h:
+//   S_0 = K_00,  G_k = K_{k,k-1} S_{k-1}^-1,  S_k = K_kk - G_k K_{k,k-1}'
+// with the pivot blocks inverted explicitly (symmetric sweep operator).  A
+// solve is then
+//   c_k = b_k - G_k c_{k-1}  (forward),  d_k = S_k^-1 c_k,
+//   x_k = d_k - G_{k+1}' x_{k+1}  (backward),
+// 2 (nb - 1) dependent block steps of dense products.  z~ = A x~ as in the
+// reduced form of the builtin's solve (qdldl_interface.c:431-466 gives the
+// same x~ and z~ in exact arithmetic).
+//
+// Everything is deterministic: each entry has one owner thread and a fixed
+// summation order, so a QP's factor and solutions do not depend on the rest
+// of a batch.  A pivot that is not positive and finite means K is not
+// positive definite (the builtin's non-convexity test, qdldl_interface.c:
+// 334-342, counts the positive pivots of the same factorisation).
+#pragma once
+
+#include "gb_common.cuh"
+#include "gb_kkt_plan.h"
+
+namespace gb {
+
+// Lanes per row of the dense block products.
+constexpr int kKktLanes = 8;
+
+template <typename T>
+struct KktView {
+  int nb = 0, bmax = 0;          // nb == 0: no direct solve
+  const int* bs = nullptr;       // [nb + 1]
+  const int* fo = nullptr;       // [nb + 1]
+  const int* co = nullptr;       // [nb + 1] (positions in cr)
+  const int* cr = nullptr;
+  const int* perm = nullptr;     // permuted position -> variable
+  const int* iperm = nullptr;    // variable -> permuted position
+  T* F = nullptr;                // factor
+};
+
+// Factor K = P + sigma I + A' R A (scaled data) into F.  ws: on-chip
+// workspace of kkt_factor_ws_elems(bmax) elements.  rho_vec == nullptr: the
+// scalar rho.  Returns false when a pivot is not positive (K not positive
+// definite in this precision).  All threads of the CTA call it.
+template <typename T>
+__device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, const CSR<T>& A, const CSR<T>& At,
+                                        const T* rho_vec, T rho_s, T sigma, T* ws) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  const int bm = kv.bmax;
+  T* Sprev = ws;
+  T* S = Sprev + bm * bm;
+  T* S2 = S + bm * bm;
+  T* Kc = S2 + bm * bm;
+  T* G = Kc + bm * bm;
+  T* tile = G + bm * bm;
+  T* rhot = tile + kKktTileRows * 2 * bm;
+  for (int k = 0; k < kv.nb; k++) {
+    const int s0 = kv.bs[k], e0 = kv.bs[k + 1], b = e0 - s0;
+    const int sp = k ? kv.bs[k - 1] : s0, bp = s0 - sp;
+    const int W = bp + b;   // assembly columns: permuted positions [sp, e0)
+    // ---- A' R A over the block's columns from the rows of A with two or
+    // more entries, in chunks of kKktTileRows rows; every output entry has
+    // one owner thread, so the sum order is fixed ----
+    T acc[kKktOutMax];
+#pragma unroll
+    for (int q = 0; q < kKktOutMax; q++) acc[q] = T(0);
+    const int nout = b * W;
+    const int c0 = kv.co[k], c1 = kv.co[k + 1];
+    for (int cb = c0; cb < c1; cb += kKktTileRows) {
+      const int nr = min(kKktTileRows, c1 - cb);
+      for (int e = tid; e < nr * W; e += nt) tile[e] = T(0);
+      __syncthreads();
+      for (int r = warp; r < nr; r += nwarps) {
+        const int row = kv.cr[cb + r];
+        const int kb = A.rowptr[row], ke = A.rowptr[row + 1];
+        for (int f = kb + lane; f < ke; f += 32) {
+          const int p = kv.iperm[A.col[f]] - sp;
+          if (p >= 0 && p < W) tile[r * W + p] = A.val[f];
+        }
+        if (lane == 0) rhot[r] = rho_vec ? rho_vec[row] : rho_s;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < kKktOutMax; q++) {
+        const int o = tid + q * nt;
+        if (o < nout) {
+          const int i = o / W, j = o - i * W;
+          T a = acc[q];
+          // (a_ri a_rj) rho_r: the same product for (i, j) and (j, i)
+          for (int r = 0; r < nr; r++) a += (tile[r * W + bp + i] * tile[r * W + j]) * rhot[r];
+          acc[q] = a;
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < kKktOutMax; q++) {
+      const int o = tid + q * nt;
+      if (o < nout) {
+        const int i = o / W, j = o - i * W;
+        if (j < bp) Kc[i * bp + j] = acc[q];
+        else S[i * b + (j - bp)] = acc[q];
+      }
+    }
+    __syncthreads();
+    // ---- P entries, sigma, and rows of A with a single entry ----
+    for (int i = tid; i < b; i += nt) {
+      const int v = kv.perm[s0 + i];
+      for (int e = P.rowptr[v]; e < P.rowptr[v + 1]; e++) {
+        const int p = kv.iperm[P.col[e]];
+        if (p >= sp && p < s0) Kc[i * bp + (p - sp)] += P.val[e];
+        else if (p >= s0 && p < e0) S[i * b + (p - s0)] += P.val[e];
+      }
+      T d = S[i * b + i] + sigma;
+      for (int e = At.rowptr[v]; e < At.rowptr[v + 1]; e++) {
+        const int row = At.col[e];
+        if (A.rowptr[row + 1] - A.rowptr[row] == 1) {
+          const T a = At.val[e];
+          d += (a * a) * (rho_vec ? rho_vec[row] : rho_s);
+        }
+      }
+      S[i * b + i] = d;
+    }
+    __syncthreads();
+    T* Fk = kv.F + kv.fo[k];
+    if (k > 0) {
+      // ---- G_k = K_{k,k-1} S_{k-1}^-1 ; S_k -= G_k K_{k,k-1}' (lower
+      // triangle, mirrored: S_k stays exactly symmetric) ----
+      for (int o = tid; o < b * bp; o += nt) {
+        const int i = o / bp, j = o - i * bp;
+        T a = T(0);
+        for (int l = 0; l < bp; l++) a += Kc[i * bp + l] * Sprev[l * bp + j];
+        G[o] = a;
+      }
+      __syncthreads();
+      for (int o = tid; o < b * b; o += nt) {
+        const int i = o / b, j = o - i * b;
+        if (j > i) continue;
+        T a = T(0);
+        for (int l = 0; l < bp; l++) a += G[i * bp + l] * Kc[j * bp + l];
+        const T v = S[i * b + j] - a;
+        S[i * b + j] = v;
+        S[j * b + i] = v;
+      }
+      T* Gg = Fk + b * b;
+      T* GTg = Gg + b * bp;
+      for (int o = tid; o < b * bp; o += nt) {
+        Gg[o] = G[o];
+        const int j = o / b, i = o - j * b;   // G' is bp x b
+        GTg[o] = G[i * bp + j];
+      }
+      __syncthreads();
+    }
+    // ---- S_k^-1 by symmetric sweeps (double-buffered): -S^-1 after b sweeps ----
+    T* src = S;
+    T* dst = S2;
+    bool bad = false;
+    for (int kk = 0; kk < b; kk++) {
+      const T piv = src[kk * b + kk];
+      if (!(piv > T(0)) || !isfinite((double)piv)) { bad = true; break; }   // CTA-uniform
+      const T d = T(1) / piv;
+      for (int o = tid; o < b * b; o += nt) {
+        const int i = o / b, j = o - i * b;
+        const T aik = src[i * b + kk], akj = src[kk * b + j];
+        T v;
+        if (i == kk) v = (j == kk) ? -d : akj * d;
+        else if (j == kk) v = aik * d;
+        else v = src[o] - (aik * akj) * d;
+        dst[o] = v;
+      }
+      __syncthreads();
+      T* t = src; src = dst; dst = t;
+    }
+    if (bad) {
+      __syncthreads();
+      return false;
+    }
+    for (int o = tid; o < b * b; o += nt) {
+      const T v = -src[o];
+      Fk[o] = v;
+      Sprev[o] = v;
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// fn(r, sum_j M[r][j] v[j]) for the rows r < rows of a row-major rows x cols
+// block, by sub-warps of kKktLanes lanes over threads [t0, t0 + tn); fn runs
+// on the sub-warp's first lane.  Loop bounds are uniform over each warp (t0
+// and tn multiples of 32).
+template <typename T, typename FN>
+__device__ __forceinline__ void kkt_block_rows(const T* __restrict__ M, const T* v, int rows, int cols, int t0,
+                                               int tn, FN fn) {
+  const int t = threadIdx.x - t0;
+  const int sub = t / kKktLanes, sl = t % kKktLanes;
+  const int per = tn / kKktLanes;
+  for (int base = 0; base < rows; base += per) {
+    const int r = base + sub;
+    T a = T(0);
+    if (r < rows) {
+      const T* Mr = M + (size_t)r * cols;
+      for (int j = sl; j < cols; j += kKktLanes) a += Mr[j] * v[j];
+    }
+    a = subwarp_sum<kKktLanes>(a);
+    if (r < rows && sl == 0) fn(r, a);
+  }
+}
+
+// Solve K x = b with the factor: c holds the permuted right-hand side on entry
+// (c[iperm[i]] = b_i); d is a second permuted n-vector; x (unpermuted) is
+// written through xout(i, value).  All threads of the CTA call it; blockDim.x
+// is a multiple of 64.
+template <typename T, typename XO>
+__device__ void kkt_solve(const KktView<T>& kv, T* c, T* d, XO xout) {
+  const int nt = blockDim.x, half = nt >> 1;
+  const bool lo = (int)threadIdx.x < half;
+  const int nb = kv.nb;
+  // forward: c_k -= G_k c_{k-1} (lower half) while d_{k-1} = S_{k-1}^-1 c_{k-1} (upper half)
+  for (int k = 1; k < nb; k++) {
+    const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+    if (lo) {
+      const T* G = kv.F + kv.fo[k] + b * b;
+      kkt_block_rows(G, c + sp, b, bp, 0, half, [&](int r, T a) { c[s0 + r] -= a; });
+    } else {
+      const T* Si = kv.F + kv.fo[k - 1];
+      kkt_block_rows(Si, c + sp, bp, bp, half, nt - half, [&](int r, T a) { d[sp + r] = a; });
+    }
+    __syncthreads();
+  }
+  {
+    const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
+    kkt_block_rows(kv.F + kv.fo[nb - 1], c + s0, b, b, 0, nt, [&](int r, T a) { d[s0 + r] = a; });
+    __syncthreads();
+  }
+  // backward: x_{k-1} = d_{k-1} - G_k' x_k (lower half) while block k is written out (upper half)
+  for (int k = nb - 1; k >= 1; k--) {
+    const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+    if (lo) {
+      const T* GT = kv.F + kv.fo[k] + b * b + b * bp;
+      kkt_block_rows(GT, d + s0, bp, b, 0, half, [&](int r, T a) { d[sp + r] -= a; });
+    } else {
+      for (int r = threadIdx.x - half; r < b; r += nt - half) xout(kv.perm[s0 + r], d[s0 + r]);
+    }
+    __syncthreads();
+  }
+  for (int r = threadIdx.x; r < kv.bs[1]; r += nt) xout(kv.perm[r], d[r]);
+  __syncthreads();
+}
+
+}  // namespace gb

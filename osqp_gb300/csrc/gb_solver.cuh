@@ -24,6 +24,7 @@
 #include <type_traits>
 
 #include "gb_common.cuh"
+#include "gb_direct.cuh"
 
 namespace gb {
 
@@ -76,6 +77,7 @@ struct SolverScalars {
   int err;
   int cancel;
   int p_parity;
+  int kkt_fail;   // direct solver: the last factorisation met a non-positive pivot
 };
 
 template <typename T>
@@ -105,6 +107,11 @@ struct DevProblem {
   T* Binv;
   const int *Arow_g, *Acol_g;
   const T* Aval_g;
+  // Direct KKT solve (linsys_solver = direct; kkt.nb == 0 otherwise): the
+  // block-tridiagonal factor and its plan (gb_direct.cuh), and the CTA's
+  // on-chip workspace for it (set by the kernel)
+  KktView<T> kkt;
+  T* kws = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -398,8 +405,9 @@ struct Solver {
   }
 
   // rho vector from constraint types (auxil.c:76-104)
+  // changed (optional): set when a constraint type differs from the stored one
   template <typename G>
-  __device__ void set_rho_vec(G& g) {
+  __device__ void set_rho_vec(G& g, int* changed = nullptr) {
     const double infval = s.infty * kMinScaling;
     const double rho = sc->rho;
     for_m(g, pr.m, [&](int j) {
@@ -408,6 +416,7 @@ struct Solver {
       if (l < -infval && u > infval) t = -1;
       else if (u - l < kRhoTol) t = 1;
       else t = 0;
+      if (changed && pr.ctype[j] != t) *changed = 1;
       pr.ctype[j] = t;
       const double rv = t < 0 ? kRhoMin : (t == 0 ? rho : kRhoEqOverIneq * rho);
       g.put(pr.rho_vec, j, (T)rv);
@@ -431,6 +440,7 @@ struct Solver {
   // and with cg_precond = 2 the inverted blocks of the block-Jacobi one
   template <typename G>
   __device__ void update_precond(G& g) {
+    if (pr.kkt.nb > 0) { direct_factor(g); return; }
     // local copies: hot loops keep the pointers in registers instead of
     // re-reading them through `this` after every store
     const DevProblem<T> pr = this->pr;
@@ -457,6 +467,19 @@ struct Solver {
       for (int b = b_lo + g.w0(); b < b_hi; b += g.ws())
         kkt_block_inverse<T>(pr.P, pr.At, pr.Arow_g, pr.Acol_g, pr.Aval_g, vec ? pr.rho_vec : nullptr, pr.Binv,
                              pr.n, b, s.sigma, sc->rho);
+    }
+  }
+
+  // Direct solver: factor K = P + sigma I + A' R A for the current rho
+  // (gb_direct.cuh).  Only the CTA form holds a plan; sc->kkt_fail records a
+  // non-positive pivot.
+  template <typename G>
+  __device__ void direct_factor(G& g) {
+    if constexpr (std::is_same<G, BlockGroup>::value) {
+      const bool ok = kkt_factor<T>(pr.kkt, pr.P, pr.A, pr.At, s.rho_is_vec ? pr.rho_vec : nullptr, (T)sc->rho,
+                                    (T)s.sigma, pr.kws);
+      if (threadIdx.x == 0) sc->kkt_fail = ok ? 0 : 1;
+      __syncthreads();
     }
   }
 
@@ -492,10 +515,11 @@ struct Solver {
       sc->rel_kkt_error = s.infty; sc->last_rel_kkt = s.infty;
       sc->rho_estimate = sc->rho; sc->primdual_int = 0.0;
       sc->zero_pcg_iters = 0; sc->reduction_factor = s.cg_tol_fraction; sc->eps_prev = 1.0;
-      sc->err = 0; sc->p_parity = 0; sc->pcg_iters_total = 0; sc->cancel = 0;
+      sc->err = 0; sc->p_parity = 0; sc->pcg_iters_total = 0; sc->cancel = 0; sc->kkt_fail = 0;
     }
     __syncthreads();
     if (!prepare_data(g, false)) return false;
+    if (threadIdx.x == 0 && pr.kkt.nb > 0 && sc->kkt_fail) sc->status = ST_NON_CVX;
     cold_start(g);
     return g.sync();
   }
@@ -516,8 +540,12 @@ struct Solver {
     const T rho_s = (T)sc->rho, rinv_s = (T)sc->rho_inv;
     T* __restrict__ x = pr.x; T* __restrict__ z = pr.z; T* __restrict__ y = pr.y;
     T* __restrict__ xp = pr.xp;
+    const bool direct = pr.kkt.nb > 0;
+    T* const kc = pr.kws;            // direct: permuted right-hand side
+    const int* const kip = pr.kkt.iperm;
 
-    // Phase R: rhs = (sigma x - q) + A'(rho .* (z - rho^-1 y)) and t = rho .* (A xp)
+    // Phase R: rhs = (sigma x - q) + A'(rho .* (z - rho^-1 y)) and, for the
+    // PCG, t = rho .* (A xp)
     Acc<T> sm0[1];
     T mx0[3] = {T(0), T(-INFINITY), T(-INFINITY)};
     rows_rng(g, span_n(g, n), pr.At,
@@ -529,10 +557,11 @@ struct Solver {
       [&](int i, T v) {
         const T b1 = sig * x[i] - pr.q[i];
         const T rr = b1 + v;
-        pr.rhs[i] = rr;
+        if (direct) kc[kip[i]] = rr;
+        else pr.rhs[i] = rr;
         mx0[0] = tmax(mx0[0], (T)fabs(rr));
       });
-    if (m > 0) {
+    if (m > 0 && !direct) {
       rows_rng(g, span_m(g, m), pr.A, [&](int c) { return xp[c]; },
         [&](int j, T v) { g.put(pr.t, j, (vec ? pr.rho_vec[j] : rho_s) * v); });
     }
@@ -549,7 +578,7 @@ struct Solver {
     const int cancel = rm0[2] > 0.0;
 
     // PCG tolerance (cuda_pcg_interface.cu:32-64), computed once per CTA
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !direct) {
       double e;
       if (iter == 1) {
         sc->reduction_factor = s.cg_tol_fraction;
@@ -570,8 +599,14 @@ struct Solver {
     __syncthreads();
     const double eps = sc->pcg_eps;
 
-    const int pcg_it = pcg_core(g, eps, sig, rho_s);
-    if (pcg_it < 0) return false;
+    if (direct) {
+      // x~ = K^-1 rhs (gb_direct.cuh), written to xp
+      if constexpr (std::is_same<G, BlockGroup>::value)
+        kkt_solve<T>(pr.kkt, kc, kc + n, [&](int i, T v) { xp[i] = v; });
+    } else {
+      const int pcg_it = pcg_core(g, eps, sig, rho_s);
+      if (pcg_it < 0) return false;
+    }
     if (threadIdx.x == 0) {
       sc->elapsed = elapsed;
       sc->cancel = cancel;
@@ -1161,6 +1196,12 @@ struct Solver {
     }
     if (it_lo <= 1 && !s.warm_starting) { cold_start(g); }
     if (!g.sync()) return false;
+    if (pr.kkt.nb > 0 && sc->kkt_fail) {
+      // the factorisation for this rho failed: K is not positive definite
+      if (threadIdx.x == 0) { sc->status = ST_NON_CVX; sc->obj_val = NAN; sc->iter = it_lo > 1 ? it_lo - 1 : 0; }
+      __syncthreads();
+      return store_solution(g);
+    }
     if (it_lo < 1) it_lo = 1;
     const int it_end = it_hi < s.max_iter ? it_hi : s.max_iter;
     int can_check = 0;
@@ -1210,6 +1251,12 @@ struct Solver {
         if (s.rho_is_vec) { refresh_rho_vec(g); if (!g.sync()) return false; }
         update_precond(g);
         if (!g.sync()) return false;
+        if (pr.kkt.nb > 0 && sc->kkt_fail) {
+          if (threadIdx.x == 0) { sc->status = ST_NON_CVX; sc->obj_val = NAN; s_flags[0] = 3; }
+          __syncthreads();
+          stopped = true;
+          break;
+        }
       }
     }
     if (!stopped && it_end < s.max_iter) {
@@ -1219,8 +1266,9 @@ struct Solver {
       return g.sync();
     }
     // post-loop (osqp_api.c:906-960); an interrupted solve skips it, as the
-    // reference jumps to its exit label on SIGINT
-    if (s_flags[0] != 2) {
+    // reference jumps to its exit label on SIGINT (and so does a failed
+    // refactorisation of the direct solver)
+    if (s_flags[0] < 2) {
       if (!can_check) {
         if (!update_info(g, iter - 1)) return false;
         if (threadIdx.x == 0) check_termination_scalar(0);
