@@ -139,8 +139,10 @@ OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** s, const OSQPMatrix* P, c
 
 /* One reduced-KKT solve that allocates nothing (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc where they solve --
- * during CUDA-graph stream capture, inside real-time loops whose memory is
- * fixed up front -- this solves (P + sigma I + A' R A) x = b1 + A' R b2 by
+ * real-time control loops whose device memory is fixed before the loop
+ * starts, because an allocation may block or fail at a moment the loop cannot
+ * afford, and programs that share the GPU under a memory budget granted up
+ * front -- this solves (P + sigma I + A' R A) x = b1 + A' R b2 by
  * PCG from x = 0 (R = diag(rho_vec), or settings->rho when rho_vec is NULL;
  * CG tolerance of the first ADMM iteration) and writes [x; A x] over b
  * (length n + m), exactly as a freshly initialised LinSysSolver's
@@ -150,10 +152,14 @@ OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** s, const OSQPMatrix* P, c
  * settings->cg_precond = 2, the ceil(n / 32) * 1024 values of the
  * block-Jacobi blocks), each rounded up to 256 bytes, must fit in 4 MiB;
  * larger problems return
- * OSQP_DATA_VALIDATION_ERROR.  The first call on a device looks up that
- * array's device address; make it before any stream capture begins.  All
- * calls share the one array: calls that overlap on the GPU (other threads,
- * other streams) race and must be serialised by the caller. */
+ * OSQP_DATA_VALIDATION_ERROR.  The call runs on the library's device (the
+ * one the matrices were created on), launches one kernel on the library's own
+ * stream and waits for it before returning.  The first call on a device looks
+ * up that array's device address; make it before any stream capture begins.
+ * All calls share the one array, which keeps the last call's contents (the
+ * kernel clears what must start at zero): calls that overlap on the GPU
+ * (other threads, other processes' streams of the same library) race and
+ * must be serialised by the caller. */
 OSQPInt osqp_gb300_linsys_solve_noalloc(const OSQPMatrix* P, const OSQPMatrix* A, const OSQPVectorf* rho_vec,
                                         const OSQPSettings* settings, OSQPVectorf* b);
 

@@ -554,3 +554,23 @@ def objective(P, q, x) -> float:
     Pu = sp.triu(P)
     Pf = Pu + sp.triu(Pu, 1).T
     return float(0.5 * x @ (Pf @ x) + q @ x)
+
+
+def kkt_plan(library: Library, P, A, bmax_limit: int = 1 << 30):
+    """Ordering of the direct KKT solver for one QP (osqp_gb300_kkt_plan; host
+    work only).  Returns (rc, block_start, perm): rc 0 on success, 1 when a
+    block exceeds bmax_limit, 2 on inconsistent input; block_start has
+    nblocks + 1 entries and perm maps permuted positions to variables."""
+    L, I = library.lib, library.I
+    fn = L.osqp_gb300_kkt_plan
+    fn.argtypes = [I, I, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I), I, C.POINTER(I), C.POINTER(I),
+                   C.POINTER(I)]
+    fn.restype = I
+    (n, _), pp, pi, _ = _csc_parts(P, library.np_float, triu=True)
+    (m, _), ap, ai, _ = _csc_parts(A, library.np_float, triu=False)
+    nb = I(0)
+    bs = np.zeros(n + 1, np.int32)
+    perm = np.zeros(n, np.int32)
+    rc = fn(n, m, _ptr(pp, I), _ptr(pi, I), _ptr(ap, I), _ptr(ai, I), bmax_limit, C.byref(nb), _ptr(bs, I),
+            _ptr(perm, I))
+    return int(rc), bs[:nb.value + 1].copy(), perm

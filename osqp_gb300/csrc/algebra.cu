@@ -955,12 +955,12 @@ extern "C" OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** sp, const OSQP
 // Allocation-free reduced-KKT solve
 //
 // For callers that cannot allocate device memory at the point of the call:
-// code running while a stream is being captured into a CUDA graph, real-time
-// control loops whose memory must be fixed before the loop starts, and hosts
-// that hand the GPU to this library only through pre-sized buffers.  The PCG
-// work vectors live in the file-scope array below (kNoAllocScratchBytes per
-// device, held by every GPU that loads the library until the process exits)
-// instead of a per-solver cudaMalloc.
+// real-time control loops whose device memory is fixed before the loop starts
+// (an allocation can block or fail at a moment the loop cannot afford), and
+// host programs that share the GPU under a memory budget granted up front.
+// The PCG work vectors live in the file-scope array below
+// (kNoAllocScratchBytes per device, held by every GPU that loads the library
+// until the process exits) instead of a per-solver cudaMalloc.
 // ---------------------------------------------------------------------------
 namespace gba {
 
@@ -1017,8 +1017,11 @@ extern "C" OSQPInt osqp_gb300_linsys_solve_noalloc(const OSQPMatrix* P, const OS
             n, m, need, kNoAllocScratchBytes);
     return OSQP_DATA_VALIDATION_ERROR;
   }
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return OSQP_ALGEBRA_LOAD_ERROR;
+  // the matrices live on the library's device: make it current, so that the
+  // scratch address and the launch belong to the same device
+  if (!ensure_ctx()) return OSQP_ALGEBRA_LOAD_ERROR;
+  const int dev = g_ctx.device;
+  if (dev < 0 || dev >= 64 || cudaSetDevice(dev) != cudaSuccess) return OSQP_ALGEBRA_LOAD_ERROR;
   // set-up, once per device, with that device current: the host-side name of
   // the array is not a device address, so ask the runtime for the address
   if (!g_noalloc_addr[dev]) {
@@ -1053,7 +1056,8 @@ extern "C" OSQPInt osqp_gb300_linsys_solve_noalloc(const OSQPMatrix* P, const OS
   d.cg_precond = (int)settings->cg_precond;
   d.infty = (double)OSQP_INFTY;
   const int kktL = pick_lanes((long long)P->nnzS + A->nnz, n);
-  cudaStream_t st = g_ctx.stream ? g_ctx.stream : (cudaStream_t)0;
+  // on the library's stream, which the call then waits for
+  cudaStream_t st = g_ctx.stream;
   k_linsys_noalloc<<<1, kLsBlockThreads, 0, st>>>(pr, d, kktL, b->d_val, (double)settings->rho);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

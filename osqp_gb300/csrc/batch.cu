@@ -681,6 +681,7 @@ static DevSettings batch_dev_settings(const OSQPSettings* st) {
   d.cg_precond = (int)st->cg_precond;
   d.scaled_termination = st->scaled_termination; d.check_dualgap = st->check_dualgap;
   d.warm_starting = st->warm_starting;
+  d.cancel_gen = 0;
   return d;
 }
 

@@ -21,6 +21,8 @@
 #include <signal.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -260,7 +262,8 @@ struct OSQPWorkspace_ {
   float last_kernel_ms;
   void* polish;           // polish workspace (gb_polish.cu)
   cudaStream_t cancel_stream;  // interrupt requests: a write of pr.st->cancel beside the running solve
-  int* h_one;                  // pinned 1, the value that write copies
+  int* h_one;                  // pinned staging of the generation that write copies
+  std::atomic<int> gen{0};     // interrupt generation: one per osqp_solve
 };
 
 // Interrupt of a running solve (osqp_api.c:728-737, interrupt_unix.c): the
@@ -270,6 +273,9 @@ struct OSQPWorkspace_ {
 // stream of its own, which runs while the solve kernel does.
 static int request_cancel(OSQPWorkspace* w) {
   if (cudaSetDevice(w->device) != cudaSuccess) return OSQP_ALGEBRA_LOAD_ERROR;
+  // the request names the generation of the solve running (or starting) now;
+  // a later solve has a newer generation, so a stale request never stops it
+  *w->h_one = w->gen.load();
   if (cudaMemcpyAsync(&w->pr.st->cancel, w->h_one, sizeof(int), cudaMemcpyHostToDevice, w->cancel_stream) != cudaSuccess ||
       cudaStreamSynchronize(w->cancel_stream) != cudaSuccess)
     return OSQP_ALGEBRA_LOAD_ERROR;
@@ -355,6 +361,7 @@ static DevSettings make_dev_settings(const OSQPSettings* st) {
   d.cg_precond = (int)st->cg_precond;
   d.scaled_termination = st->scaled_termination; d.check_dualgap = st->check_dualgap;
   d.warm_starting = st->warm_starting;
+  d.cancel_gen = 0;
   return d;
 }
 
@@ -837,8 +844,9 @@ static int launch_solve(OSQPWorkspace* w) {
   cudaStream_t s = w->stream;
   cudaMemsetAsync(w->bar, 0, sizeof(unsigned int) * 4 + sizeof(int) * 4, s);
   // an interrupt counts for the solve it arrives in (the reference's
-  // listener also starts clear on every solve)
-  GB_TRY(cudaMemsetAsync(&w->pr.st->cancel, 0, sizeof(int), s));
+  // listener also starts clear on every solve): this solve's generation is
+  // new, so the cancel word matches it only after a request made from now on
+  w->ds.cancel_gen = ++w->gen;
   cudaEventRecord(w->ev0, s);
   if (w->use_grid) {
     GridSync gs; grid_sync_args(w, gs);
@@ -903,7 +911,7 @@ extern "C" OSQPInt osqp_solve(OSQPSolver* solver) {
     bool sent = false;
     while (cudaStreamQuery(w->stream) == cudaErrorNotReady) {
       if (!sent && listener.fired()) { request_cancel(w); sent = true; }
-      std::this_thread::yield();
+      std::this_thread::sleep_for(std::chrono::microseconds(50));   // a core is not pinned per solve
     }
   }
   rc = check_device_error(w);

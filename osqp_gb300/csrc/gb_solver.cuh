@@ -51,6 +51,9 @@ struct DevSettings {
   int adaptive_rho, adaptive_rho_interval;
   int cg_max_iter, cg_tol_reduction, cg_precond;
   int scaled_termination, check_dualgap, warm_starting;
+  // interrupt generation of this solve (> 0): the solve stops when its
+  // cancel word holds this value; 0: no interrupts
+  int cancel_gen;
 };
 
 // Per-problem scalar state.  Lives in global memory between launches; during
@@ -568,7 +571,8 @@ struct Solver {
     // time / cancellation ride on this reduction so every CTA sees the same values
     if (g.tid() == 0) {
       mx0[1] = (T)((double)(global_ns() - sc->t_start) * 1e-9);
-      mx0[2] = (T)(*((volatile int*)&pr.st->cancel));
+      const int cw = *((volatile int*)&pr.st->cancel);
+      mx0[2] = (s.cancel_gen > 0 && cw == s.cancel_gen) ? T(1) : T(0);
     }
     double rs0[1], rm0[3];
     g.reduce(sm0, mx0, rs0, rm0);

@@ -1,18 +1,21 @@
 """The allocation-free reduced-KKT solve (osqp_gb300_linsys_solve_noalloc).
 
-Some callers cannot allocate device memory where they solve: code running
-while a stream is captured into a CUDA graph, or real-time loops whose memory
-is fixed before they start.  This entry point keeps its work vectors in a
-fixed device array inside the library; here it is called through the C ABI
-and checked against the regular linear-system solver (a fresh
-LinSysSolver.solve) on the same data, on two calls in a row (the second call
-sees the scratch the first one left behind).
+Some callers cannot allocate device memory where they solve: real-time loops
+whose device memory is fixed before they start (an allocation could block or
+fail mid-loop), or programs sharing a GPU under a budget granted up front.
+This entry point keeps its work vectors in a fixed device array inside the
+library; here it is called through the C ABI and checked against the regular
+linear-system solver (a fresh LinSysSolver.solve) on the same data, on two
+calls in a row (the second call sees the scratch the first one left behind),
+and against an FP64 host solve of the same system (scipy), within the error
+bound that the PCG's stopping tolerance implies.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 import scipy.sparse as sp
+import scipy.sparse.linalg  # noqa: F401
 
 pytestmark = pytest.mark.gpu
 
@@ -66,6 +69,10 @@ def test_noalloc_matches_linsys_solver(prec, vector_rho, precond):
         rhs_red = rhs[:n] + A.T @ (rv * rhs[n:])
         r = K @ x - rhs_red
         assert np.max(np.abs(r)) <= 1.05 * st.cg_tol_fraction * np.max(np.abs(rhs_red))
+        # independent FP64 solve: ||x - x*||_2 <= ||K x - rhs||_2 / lambda_min(K)
+        x_star = sp.linalg.spsolve(K.tocsc(), rhs_red)
+        lam_min = np.linalg.eigvalsh(K.toarray())[0]
+        assert np.linalg.norm(x - x_star) <= 1.01 * np.linalg.norm(r) / lam_min + TOL[prec] * np.linalg.norm(x_star)
         assert np.allclose(got[n:], A @ x, atol=TOL[prec] * max(1.0, np.max(np.abs(A @ x))))
 
 
