@@ -53,12 +53,12 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 from osqp_gb300 import problems as pb  # noqa: E402
-from osqp_gb300.roofline import solve_bytes, pfull_nnz  # noqa: E402
+from osqp_gb300.roofline import solve_bytes, direct_solve_bytes, pfull_nnz  # noqa: E402
 from osqp_gb300.api import BLOCK_DIAGONAL_PRECONDITIONER  # noqa: E402
 
 SETTINGS = dict(rho=0.1, sigma=1e-6, alpha=1.6, scaling=10, eps_abs=1e-3, eps_rel=1e-3, rho_is_vec=1,
                 check_termination=5, adaptive_rho_tolerance=5.0, max_iter=4000, check_dualgap=1,
-                warm_starting=0, polishing=0)
+                warm_starting=0, polishing=0, linsys_solver=1)
 
 
 def _nx_of(A):
@@ -80,12 +80,11 @@ def make_workload(count, steps, seed=3):
     return probs, ls, us
 
 
-# DRAM bytes per algorithmic byte of the CTA-form solve launch, from the ncu
-# capture of 304 batched MPC QPs (profiles/k_batch_solve_mpc304.md:
-# 52.2 + 7.0 GB DRAM for 285.6 GB algorithmic).  The 4096-QP launch is too
-# long to capture under the size rule; its traffic is this ratio times its
-# algorithmic bytes (the matrices of the QPs in flight stay L2-resident in both).
-TRAFFIC_PER_ALGORITHMIC_BYTE = (52.202385 + 6.987452) / 285.586664900
+# DRAM bytes per algorithmic byte of the solve launch, from one ncu capture
+# of a smaller batch of the same QPs (the 4096-QP launch is too long to
+# capture); the launch's traffic is this ratio times its algorithmic bytes.
+# PCG path: 304 QPs, 52.2 + 7.0 GB DRAM for 285.6 GB algorithmic.
+TRAFFIC_PER_ALGORITHMIC_BYTE = {2: (52.202385 + 6.987452) / 285.586664900, 1: None}
 
 
 def measured_peak():
@@ -150,55 +149,66 @@ class ClockSampler:
 # CPU oracle arm (the reference's builtin algorithm, FP64, direct LDL^T)
 # ---------------------------------------------------------------------------
 def _cpu_worker(args):
-    lib_path, probs, lsteps, usteps, settings = args
+    lib_path, probs, lsteps, usteps, settings, keep = args
     from osqp_gb300.api import Library, OSQP, DIRECT_SOLVER
     lib = Library(lib_path, 64)
     solvers = []
+    st = dict(settings)
+    st["linsys_solver"] = DIRECT_SOLVER
     for (P, q, A, l, u) in probs:
         s = OSQP(lib)
-        s.setup(P, q, A, l, u, linsys_solver=DIRECT_SOLVER, **settings)
+        s.setup(P, q, A, l, u, **st)
         solvers.append(s)
-    objs = []
-    t0 = time.perf_counter()
+    per_step, first = [], None
     for ls, us in zip(lsteps, usteps):
         objs = []
+        t0 = time.perf_counter()
         for s, l, u in zip(solvers, ls, us):
             s.update(l=l, u=u)
             r = s.solve()
-            objs.append((r.info["status_val"], r.info["obj_val"]))
-    return time.perf_counter() - t0, len(solvers) * len(lsteps), objs
+            objs.append((r.info["status_val"], r.info["obj_val"], r.info["iter"]))
+        per_step.append(time.perf_counter() - t0)
+        if len(per_step) == keep + 1:
+            first = objs
+    return per_step, len(solvers), first
 
 
-def cpu_arm(probs, ls, us, sizes_m, budget_s=15.0, steps=1):
-    """Oracle on all host cores: a bounded sample of QPs x steps; returns solves/s."""
+def cpu_arm(probs, ls, us, sizes_m, steps_timed, steps_warm=0):
+    """The FP64 oracle (OSQP's builtin algorithm: direct LDL' KKT solve) on all
+    host cores: every QP of the workload, one process per core, each owning a
+    contiguous share of the QPs (set up once, untimed).  A step updates every
+    QP's bounds and solves it; the step's time is the slowest process's.
+    Returns solves/s over the timed steps, the step time and, per QP, the
+    first timed step's (status, objective, iterations)."""
     lib_path = os.path.join(REPO, "oracle", "_build", "liboracle.so")
     if not os.path.exists(lib_path):
         subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "port"], check=True)
     cores = os.cpu_count() or 1
     moff = np.concatenate([[0], np.cumsum(sizes_m)])
-    # sample size: roughly budget_s of work; calibrate on one QP per core
-    sample = min(len(probs), max(cores, 4 * cores))
-    idx = list(range(sample))
-    chunks = [idx[c::cores] for c in range(cores) if idx[c::cores]]
+    count = len(probs)
+    # contiguous shares balanced by size (nonzeros of A)
+    work = np.array([p[2].nnz for p in probs], dtype=np.float64)
+    cuts = np.searchsorted(np.cumsum(work), np.linspace(0, work.sum(), cores + 1)[1:-1])
+    chunks = [list(c) for c in np.split(np.arange(count), cuts) if len(c)]
+    nsteps = steps_warm + steps_timed
     tasks = []
     for ch in chunks:
         pp = [probs[i] for i in ch]
-        lst = [[ls[s][moff[i]:moff[i + 1]] for i in ch] for s in range(steps)]
-        ust = [[us[s][moff[i]:moff[i + 1]] for i in ch] for s in range(steps)]
-        tasks.append((lib_path, pp, lst, ust, dict(SETTINGS)))
+        lst = [[ls[s][moff[i]:moff[i + 1]] for i in ch] for s in range(nsteps)]
+        ust = [[us[s][moff[i]:moff[i + 1]] for i in ch] for s in range(nsteps)]
+        tasks.append((lib_path, pp, lst, ust, dict(SETTINGS), steps_warm))
     ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
     with ctx.Pool(len(tasks)) as pool:
         res = pool.map(_cpu_worker, tasks)
-    wall = time.perf_counter() - t0
-    solved = sum(r[1] for r in res)
-    busy = max(r[0] for r in res)
-    objs = {}
+    step_s = [max(r[0][s] for r in res) for s in range(steps_warm, nsteps)]
+    first = {}
     for ch, r in zip(chunks, res):
         for i, o in zip(ch, r[2]):
-            objs[i] = o
-    return {"value": solved / busy, "cores": len(tasks), "sample": f"{sample} MPC QPs x {steps} step(s)",
-            "wall_s": wall, "objs": objs}
+            first[i] = o
+    total = float(np.sum(step_s))
+    return {"value": count * steps_timed / total, "cores": len(tasks), "ms_per_step": 1e3 * total / steps_timed,
+            "sample": f"all {count} MPC QPs x {steps_timed} step(s) (every QP of the step)",
+            "first": first, "step_s": step_s}
 
 
 # ---------------------------------------------------------------------------
@@ -274,7 +284,9 @@ def gpu_arm(args, probs, ls, us):
     barrier(); torch.cuda.synchronize()
     clocks.start()
     step_ms, solve_ms, bytes_alg = [], [], 0.0
-    obj_first = None
+    first = None
+    direct = SETTINGS["linsys_solver"] == 1
+    felems = b.factor_elems() if direct else None
     admm_tot = pcg_tot = 0
     nnz_pf = [pfull_nnz(p[0]) for p in probs]
     launches = 0
@@ -287,14 +299,19 @@ def gpu_arm(args, probs, ls, us):
         st = b.stats()
         solve_ms.append(st["kernel_ms"])
         sol = b.solution()
-        if obj_first is None:
-            obj_first = sol["obj"].copy()   # step W: the step the CPU sample solves
+        if first is None:   # step W: the step the CPU oracle solves
+            first = {"status": sol["status"].copy(), "obj": sol["obj"].copy(), "iter": sol["iter"].copy()}
         pcg = b.pcg_iters()
+        rup = b.rho_updates() if direct else None
         admm_tot += int(sol["iter"].sum()); pcg_tot += int(pcg.sum())
         for k, (P, q, A, l, u) in enumerate(probs):
-            bytes_alg += solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, 4, int(sol["iter"][k]),
-                                     int(pcg[k]), SETTINGS["check_termination"],
-                                     SETTINGS.get("cg_precond", 1) == BLOCK_DIAGONAL_PRECONDITIONER)
+            if direct:
+                bytes_alg += direct_solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, 4, int(sol["iter"][k]),
+                                                int(felems[k]), int(rup[k]), SETTINGS["check_termination"])
+            else:
+                bytes_alg += solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, 4, int(sol["iter"][k]),
+                                         int(pcg[k]), SETTINGS["check_termination"],
+                                         SETTINGS.get("cg_precond", 1) == BLOCK_DIAGONAL_PRECONDITIONER)
     torch.cuda.synchronize(); barrier()
     clk = clocks.stop()
     status_last = sol["status"].copy()
@@ -347,9 +364,29 @@ def gpu_arm(args, probs, ls, us):
         bytes_per_launch=bytes_alg / K,
         admm_per_qp=admm_tot / (count * K), pcg_per_qp=pcg_tot / (count * K),
         status_counts={int(k): int(v) for k, v in zip(*np.unique(status_last, return_counts=True))},
-        obj_last=obj_first, launches=launches, clocks=clk, plain=plain, rank=rank, world=world, tile=tile,
+        first=first, launches=launches, clocks=clk, plain=plain, rank=rank, world=world, tile=tile,
+        factor_bytes=float(np.sum(felems)) * 4 if direct else None,
     )
+    b.cleanup()
     return out
+
+
+def indirect_leg(probs, ls, us, W):
+    """The PCG path (the reference CUDA backend's algorithm) on the same
+    batch: one warm-up and one timed step, device time."""
+    from osqp_gb300 import load
+    from osqp_gb300.api import Batch
+    b = Batch(load("f32"))
+    assert b.setup(probs, **dict(SETTINGS, linsys_solver=2)) == 0
+    b.update(l=ls[0], u=us[0]); b.solve()
+    b.update(l=ls[W], u=us[W]); b.solve()
+    ms = b.step_ms()
+    st = b.stats()
+    sol = b.solution()
+    b.cleanup()
+    return {"solves_per_s": len(probs) / (ms * 1e-3), "ms_per_step": ms, "admm_iters_per_qp": st["admm_iter"] / len(probs),
+            "pcg_iters_per_qp": st["pcg_iter"] / len(probs),
+            "status_counts": {int(k): int(v) for k, v in zip(*np.unique(sol["status"], return_counts=True))}}
 
 
 # ---------------------------------------------------------------------------
@@ -373,7 +410,7 @@ def _oracle_job(args_):
     from osqp_gb300.api import Library, OSQP
     s = OSQP(Library(lib_path, 64))
     P, q, A, l, u = data
-    s.setup(P, q, A, pb.clip_inf(l, 1e30), pb.clip_inf(u, 1e30), linsys_solver=linsys, **settings)
+    s.setup(P, q, A, pb.clip_inf(l, 1e30), pb.clip_inf(u, 1e30), **dict(settings, linsys_solver=linsys))
     t = time.perf_counter()
     r = s.solve()
     return time.perf_counter() - t, r.x, r.y, r.info["status"], r.info["iter"], r.info["status_polish"]
@@ -386,12 +423,13 @@ def single_config(args):
     torch.cuda.set_device(0)
     if args.config == "large_sparse":
         data = pb.large_sparse()
-        st = dict(SETTINGS, warm_starting=0, polishing=0)
+        st = dict(SETTINGS, warm_starting=0, polishing=0, linsys_solver=INDIRECT_SOLVER)
         oracle_linsys = INDIRECT_SOLVER
         desc = "large_sparse: n=50,000, m=100,000, P=MM'+1e-2I (8 nnz/col of M), A 10 nnz/row, eps 1e-3"
     else:
         data = pb.svm()
-        st = dict(SETTINGS, eps_abs=1e-5, eps_rel=1e-5, warm_starting=0, polishing=1, max_iter=20000)
+        st = dict(SETTINGS, eps_abs=1e-5, eps_rel=1e-5, warm_starting=0, polishing=1, max_iter=20000,
+                  linsys_solver=INDIRECT_SOLVER)
         oracle_linsys = DIRECT_SOLVER
         desc = "svm: m=100,000 samples x 1,000 features, 15% density, lambda=1, eps 1e-5, polish"
     P, q, A, l, u = data
@@ -467,9 +505,11 @@ def serve_leg(args):
     port = [pb.portfolio(seed=20000 + i) for i in range(S)]
     st = dict(SETTINGS, warm_starting=1)
     pools = []
-    for probs in (mpc, port):
+    # MPC requests take the configured solver; portfolio QPs (a budget row over
+    # every asset: one dense block) always take the PCG
+    for probs, ls_ in ((mpc, SETTINGS["linsys_solver"]), (port, 2)):
         b = Batch(lib)
-        assert b.setup(probs, **st) == 0, "pool set-up refused"
+        assert b.setup(probs, **dict(st, linsys_solver=ls_)) == 0, "pool set-up refused"
         pools.append(b)
     srv = Server(lib, concurrency=args.serve_concurrency)
     pid = [srv.add_pool(b) for b in pools]
@@ -540,7 +580,6 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--count", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=64)
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="served form: Poisson arrivals (req/s); 0 = skip")
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--serve-streams", type=int, default=128, help="recurring problems per class")
@@ -552,8 +591,14 @@ def main():
                     help="ADMM iteration cap (smaller values give short profiling cases)")
     ap.add_argument("--precond", default="diagonal", choices=["diagonal", "block"],
                     help="PCG preconditioner: OSQP's diagonal (Jacobi) one or the 32 x 32 block-Jacobi one")
+    ap.add_argument("--linsys", default="direct", choices=["direct", "indirect"],
+                    help="linear-system solver of the batched engine (direct: block-tridiagonal LDL'; "
+                         "indirect: the reduced-KKT PCG)")
+    ap.add_argument("--indirect-compare", type=int, default=1, help="also time one step of the PCG path")
+    ap.add_argument("--cpu-oracle", type=int, default=1, help="FP64 CPU oracle over every QP of one step")
     args = ap.parse_args()
     SETTINGS["max_iter"] = args.max_iter
+    SETTINGS["linsys_solver"] = 1 if args.linsys == "direct" else 2
     if args.precond == "block":
         SETTINGS["cg_precond"] = BLOCK_DIAGONAL_PRECONDITIONER
     if args.config != "mpc_batch":
@@ -566,22 +611,25 @@ def main():
                           "new x0 per step, cold solve to eps 1e-3",
               "qps_per_step": args.count, "eps": 1e-3, "settings": "rho_is_vec=1, check_termination=5, "
               "adaptive_rho, scaling=10, check_dualgap=1",
-              "preconditioner": "block-Jacobi 32x32" if args.precond == "block" else "diagonal (Jacobi)", "l2": "inputs (~3 GB of CSR data) exceed the 129 MB L2",
+              "linsys_solver": args.linsys,
+              "preconditioner": ("block-Jacobi 32x32" if args.precond == "block" else "diagonal (Jacobi)") if args.linsys == "indirect" else None,
+              "l2": "inputs (~3 GB of CSR data and factors) exceed the 129 MB L2",
               "parallelism": f"replicas x{world}"}
     metric = "QP solves/s (batched MPC, eps 1e-3)"
 
     if args.impl == "reference":
         if rank != 0:
             return
-        probs, ls, us = make_workload(args.count, 1)
+        probs, ls, us = make_workload(args.count, K + W)
         sizes_m = [p[2].shape[0] for p in probs]
-        cpu = cpu_arm(probs, ls, us, sizes_m, budget_s=args.cpu_budget, steps=1)
+        cpu = cpu_arm(probs, ls, us, sizes_m, steps_timed=K, steps_warm=W)
         line = dict(metric=metric, value=cpu["value"], unit="solves/s", n_gpus=args.gpus, steps=K, warmup=W,
-                    ms_per_step=args.count / cpu["value"] * 1e3, higher_is_better=True, scaling="weak",
+                    ms_per_step=cpu["ms_per_step"], higher_is_better=True, scaling="weak",
                     vs_baseline=None, dtype="f64", data="synthetic (seeded)", config=config, impl="reference",
                     cpu_baseline={"value": cpu["value"], "unit": "solves/s", "cores": cpu["cores"], "kind": "port",
                                   "sample": cpu["sample"]},
-                    e2e={"value": cpu["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+                    e2e={"value": cpu["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                    step_seconds=cpu["step_s"])
         print(json.dumps(line))
         return
 
@@ -589,19 +637,34 @@ def main():
     g = gpu_arm(args, probs, ls, us)
     if rank != 0:
         return
+    direct = SETTINGS["linsys_solver"] == 1
+    indirect = indirect_leg(probs, ls, us, W) if (direct and args.indirect_compare) else None
     served = serve_leg(args) if args.serve_rate > 0 else None
     peak, peak_kind = measured_peak()
     sizes_m = [p[2].shape[0] for p in probs]
-    cpu = cpu_arm(probs, [ls[W]], [us[W]], sizes_m, budget_s=args.cpu_budget, steps=1) if args.cpu_budget > 0 else None
-    # objective agreement with the FP64 oracle on the CPU sample (same QPs, same step)
-    obj_err = None
+    # the FP64 oracle on the host cores: every QP of the first timed step
+    cpu = cpu_arm(probs, [ls[W]], [us[W]], sizes_m, steps_timed=1) if args.cpu_oracle else None
+    parity = None
     if cpu:
-        errs = []
-        for i, (stat, obj) in cpu["objs"].items():
-            if stat == 1 and i < len(g["obj_last"]):
-                errs.append(abs(float(g["obj_last"][i]) - obj) / max(1.0, abs(obj)))
-        obj_err = {"max_rel": float(np.max(errs)) if errs else None,
-                   "median_rel": float(np.median(errs)) if errs else None, "qps": len(errs)}
+        f = g["first"]
+        st_g, st_o = f["status"], np.array([cpu["first"][i][0] for i in range(len(probs))])
+        errs, ratio = [], []
+        for i in range(len(probs)):
+            if st_o[i] == 1 and st_g[i] == 1:
+                oo = cpu["first"][i][1]
+                errs.append(abs(float(f["obj"][i]) - oo) / max(1.0, abs(oo)))
+                ratio.append(float(f["iter"][i]) / max(1, cpu["first"][i][2]))
+        errs, ratio = np.array(errs), np.array(ratio)
+        parity = {"qps": len(probs), "status_mismatches": int(np.sum(st_g != st_o)),
+                  "objective_rel_err": {"max": float(errs.max()), "p99": float(np.percentile(errs, 99)),
+                                        "median": float(np.median(errs)),
+                                        "fraction_le_1e-4": float(np.mean(errs <= 1e-4))},
+                  "admm_iteration_ratio": {"median": float(np.median(ratio)),
+                                           "fraction_equal": float(np.mean(ratio == 1.0)),
+                                           "fraction_within_10pct": float(np.mean(np.abs(ratio - 1) <= 0.1))},
+                  "oracle_admm_iters_per_qp": float(np.mean([cpu["first"][i][2] for i in range(len(probs))])),
+                  "against": "FP64 oracle, builtin algorithm (direct LDL' KKT solve), same QPs and step"}
+    tr = TRAFFIC_PER_ALGORITHMIC_BYTE[SETTINGS["linsys_solver"]]
     line = dict(
         metric=metric, value=g["value"], unit="solves/s", n_gpus=world, steps=K, warmup=W,
         ms_per_step=g["ms_per_step"], higher_is_better=True, scaling="weak", vs_baseline=None,
@@ -610,18 +673,21 @@ def main():
              "d2h_bytes_per_step": g["d2h"]},
         roofline={"bound": "hbm", "achieved": g["achieved_gbs"], "peak": peak, "unit": "GB/s",
                   "frac": g["achieved_gbs"] / peak,
-                  "traffic": TRAFFIC_PER_ALGORITHMIC_BYTE * g["bytes_per_launch"],
-                  "traffic_source": "ncu capture of 304 QPs (dram read+write / algorithmic bytes = "
-                                    f"{TRAFFIC_PER_ALGORITHMIC_BYTE:.3f}) scaled to this launch's algorithmic bytes",
+                  "traffic": (tr * g["bytes_per_launch"]) if tr else None,
+                  "traffic_source": (f"ncu capture of a smaller batch (dram read+write / algorithmic bytes = {tr:.3f})"
+                                     " scaled to this launch's algorithmic bytes") if tr else "not captured",
                   "kernel": "k_batch (solve)", "peak_source": peak_kind,
-                  "algorithmic_bytes_per_launch": g["bytes_per_launch"], "kernel_ms": g["solve_ms"]},
+                  "algorithmic_bytes_per_launch": g["bytes_per_launch"], "kernel_ms": g["solve_ms"],
+                  "factor_bytes": g["factor_bytes"]},
         cpu_baseline=None if not cpu else {"value": cpu["value"], "unit": "solves/s", "cores": cpu["cores"],
                                            "kind": "port", "sample": cpu["sample"]},
         clocks=g["clocks"], gpu_launches=g["launches"],
+        linsys_solver="direct (block-tridiagonal LDL')" if direct else "indirect (reduced-KKT PCG)",
         plain_gpu_solves_per_s=g["plain"],
         batched_over_plain=(g["value"] / g["plain"]) if g["plain"] else None,
         admm_iters_per_qp=g["admm_per_qp"], pcg_iters_per_qp=g["pcg_per_qp"],
-        status_counts=g["status_counts"], objective_vs_fp64_oracle=obj_err,
+        status_counts=g["status_counts"], parity_vs_fp64_oracle=parity,
+        indirect=indirect,
         spmv_tile_entries_per_lane=g["tile"],
         served=served,
     )

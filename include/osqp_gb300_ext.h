@@ -128,6 +128,15 @@ OSQPInt osqp_gb300_batch_qp_seconds(OSQPBatch* batch, double* seconds);
 /* PCG iterations of every QP in the last batch solve (count entries, host memory). */
 OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* batch, long long* pcg_iter);
 
+/* rho updates of every QP in the last batch solve (count entries, host memory;
+ * OSQPInfo.rho_updates, include/public/osqp_api_types.h:165). */
+OSQPInt osqp_gb300_batch_rho_updates(OSQPBatch* batch, OSQPInt* rho_updates);
+
+/* Elements of every QP's direct-solver factor (count entries, host memory; 0
+ * for the indirect solver): the bytes one direct solve reads, over the value
+ * width.  No reference counterpart. */
+OSQPInt osqp_gb300_batch_factor_elems(OSQPBatch* batch, long long* elems);
+
 OSQPInt osqp_gb300_batch_cleanup(OSQPBatch* batch);
 
 /* Ordering of the direct solver for one QP (host memory; no device work):

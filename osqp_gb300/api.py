@@ -355,6 +355,10 @@ class Batch:
         L.osqp_gb300_batch_autotune.restype = I
         L.osqp_gb300_batch_qp_seconds.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.osqp_gb300_batch_qp_seconds.restype = I
+        L.osqp_gb300_batch_rho_updates.argtypes = [C.c_void_p, PI]
+        L.osqp_gb300_batch_rho_updates.restype = I
+        L.osqp_gb300_batch_factor_elems.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+        L.osqp_gb300_batch_factor_elems.restype = I
 
     @staticmethod
     def pack(problems, float_dtype):
@@ -451,6 +455,17 @@ class Batch:
     def pcg_iters(self):
         out = np.zeros(self.count, np.int64)
         self.L.lib.osqp_gb300_batch_pcg_iters(self._h, out.ctypes.data_as(C.POINTER(C.c_longlong)))
+        return out
+
+    def rho_updates(self):
+        out = np.zeros(self.count, np.int32)
+        self.L.lib.osqp_gb300_batch_rho_updates(self._h, out.ctypes.data_as(C.POINTER(self.L.I)))
+        return out
+
+    def factor_elems(self):
+        """Elements of each QP's direct-solver factor (0 with the indirect solver)."""
+        out = np.zeros(self.count, np.int64)
+        self.L.lib.osqp_gb300_batch_factor_elems(self._h, out.ctypes.data_as(C.POINTER(C.c_longlong)))
         return out
 
     def stats(self):

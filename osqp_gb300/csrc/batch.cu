@@ -306,7 +306,11 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   // direct KKT solve: the dynamic shared memory is the factorisation's and the
   // block solve's workspace (the QP's data stay in HBM / L2)
   const bool direct = pv.kkt.nb > 0;
-  if (direct) pv.kws = (TT*)dsm;
+  if (direct) {
+    pv.kws = (TT*)dsm;
+    kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.kkt.bmax) * sizeof(TT)));
+    __syncthreads();
+  }
   if (mode == kModeSolve && dsm_bytes > 0 && !direct) {
     if constexpr (std::is_same<G, ClusterGroup>::value) {
       // block-Jacobi needs each block of r in one CTA: n-slices start on block boundaries
@@ -520,7 +524,7 @@ __global__ void k_batch_check_bounds(const TT* l, const TT* u, long long msum, i
     if (l[j] > u[j]) atomicExch(bad, 1);
 }
 
-struct BatchInfo { int status, iter; long long pcg; double obj, prim, dual, seconds; };
+struct BatchInfo { int status, iter; long long pcg; double obj, prim, dual, seconds; int rho_updates, pad; };
 
 __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out, long long* totals) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
@@ -531,6 +535,7 @@ __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out,
     out[k].prim = st[k].prim_res;
     out[k].dual = st[k].dual_res;
     out[k].seconds = st[k].elapsed;
+    out[k].rho_updates = st[k].rho_updates;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     long long a = 0, p = 0;
@@ -612,6 +617,7 @@ static int env_int(const char* name, int dflt) {
 struct OSQPBatch_ {
   int count, device;
   int direct;             // linsys_solver = direct: every QP has a KKT plan
+  long long kf_total;     // direct: factor elements of the whole batch
   long long nsum, msum, nnzT, nnzA, nnzPf;
   size_t binv_elems;    // block-Jacobi storage (0 unless cg_precond = 2)
   cudaStream_t stream;
@@ -872,7 +878,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
           const BatchInst& I = b->inst[k];
           prc[k] = kkt_plan_build(I.n, I.m, hPp.data() + pp_off[k], hPi.data() + I.pt_off, hAp.data() + pp_off[k],
                                   hAi.data() + I.a_off, blim, plans[k]);
-          if (!prc[k] && kkt_ws_elems(I.n, plans[k].bmax) * (long long)sizeof(T) > b->dsm) prc[k] = 3;
+          if (!prc[k] && kkt_ws_bytes(I.n, plans[k].bmax, plans[k].nb, (int)sizeof(T)) > b->dsm) prc[k] = 3;
         }
       });
     for (auto& th : pool) th.join();
@@ -891,6 +897,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
       kb_tot += plans[k].nb + 1; kcr_tot += (long long)plans[k].cr.size(); kf_tot += plans[k].fsize;
     }
     if (kb_tot > INT32_MAX || kcr_tot > INT32_MAX) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
+    b->kf_total = kf_tot;
   } else {
     for (int k = 0; k < count; k++) { BatchInst& I = b->inst[k]; I.knb = 0; I.kbmax = 0; I.kb_off = 0; I.kcr_off = 0; I.kf_off = 0; }
   }
@@ -1283,6 +1290,21 @@ extern "C" OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* b, long long* pcg) {
   std::vector<BatchInfo> info(b->count);
   BT_TRY(cudaMemcpy(info.data(), b->d_info, sizeof(BatchInfo) * b->count, cudaMemcpyDeviceToHost));
   for (int k = 0; k < b->count; k++) pcg[k] = info[k].pcg;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_rho_updates(OSQPBatch* b, OSQPInt* rho_updates) {
+  if (!b || !rho_updates) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  std::vector<BatchInfo> info(b->count);
+  BT_TRY(cudaMemcpy(info.data(), b->d_info, sizeof(BatchInfo) * b->count, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < b->count; k++) rho_updates[k] = info[k].rho_updates;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_factor_elems(OSQPBatch* b, long long* elems) {
+  if (!b || !elems) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  for (int k = 0; k < b->count; k++)
+    elems[k] = b->direct ? ((k + 1 < b->count ? b->inst[k + 1].kf_off : b->kf_total) - b->inst[k].kf_off) : 0;
   return 0;
 }
 

@@ -33,6 +33,7 @@
 #include "gb_structure.cuh"
 #include "gb_launch.cuh"
 #include "gb_engine.h"
+#include "gb_kkt_plan.h"
 
 using T = OSQPFloat;
 using namespace gb;
@@ -59,12 +60,26 @@ static double wall_s() {
 constexpr int kBlockThreads = 1024;
 constexpr int kGridThreads = 1024;
 
+// Dynamic shared memory of the CTA form: the direct solver's workspace
+// (gb_direct.cuh; empty for the indirect solver).
+extern __shared__ __align__(16) unsigned char g_engine_dsm[];
+
+template <typename TT>
+__device__ __forceinline__ void attach_direct_ws(DevProblem<TT>& pr) {
+  if (pr.kkt.nb > 0) {
+    pr.kws = (TT*)g_engine_dsm;
+    kkt_plan_on_chip(pr.kkt, (int*)(g_engine_dsm + kkt_ws_elems(pr.n, pr.kkt.bmax) * sizeof(TT)));
+    __syncthreads();
+  }
+}
+
 template <typename TT>
 __global__ void __launch_bounds__(kBlockThreads, 1)
 k_setup_block(DevProblem<TT> pr, DevSettings s, int kktL, int keep_state) {
   __shared__ GroupShared gsh;
   __shared__ SolverScalars ssc;
   if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (keep_state) ssc = *pr.st; }
+  attach_direct_ws(pr);
   __syncthreads();
   BlockGroup g{&gsh};
   Solver<TT> S{pr, s, &ssc, kktL};
@@ -79,12 +94,31 @@ k_solve_block(DevProblem<TT> pr, DevSettings s, int kktL) {
   __shared__ GroupShared gsh;
   __shared__ SolverScalars ssc;
   if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; ssc = *pr.st; }
+  attach_direct_ws(pr);
   __syncthreads();
   BlockGroup g{&gsh};
   Solver<TT> S{pr, s, &ssc, kktL};
   S.solve(g);
   __syncthreads();
   if (threadIdx.x == 0) *pr.st = ssc;
+}
+
+// Direct solver: refactor K for the rho (vector) in device memory after a
+// host-driven change of rho or of the constraint types; records a
+// non-positive pivot in the scalar state's kkt_fail.
+template <typename TT>
+__global__ void __launch_bounds__(kBlockThreads, 1)
+k_refactor_block(DevProblem<TT> pr, DevSettings s, int kktL) {
+  __shared__ GroupShared gsh;
+  __shared__ SolverScalars ssc;
+  if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; ssc = *pr.st; }
+  attach_direct_ws(pr);
+  __syncthreads();
+  BlockGroup g{&gsh};
+  Solver<TT> S{pr, s, &ssc, kktL};
+  S.update_precond(g);
+  __syncthreads();
+  if (threadIdx.x == 0) pr.st->kkt_fail = ssc.kkt_fail;
 }
 
 template <typename TT>
@@ -261,6 +295,7 @@ struct OSQPWorkspace_ {
   cudaEvent_t ev0, ev1;
   float last_kernel_ms;
   void* polish;           // polish workspace (gb_polish.cu)
+  size_t kdsm;                 // direct solver: dynamic shared memory of the CTA-form kernels
   cudaStream_t cancel_stream;  // interrupt requests: a write of pr.st->cancel beside the running solve
   int* h_one;                  // pinned staging of the generation that write copies
   std::atomic<int> gen{0};     // interrupt generation: one per osqp_solve
@@ -387,7 +422,7 @@ static void set_status(OSQPInfo* info, int s) {
 extern "C" {
 
 OSQPInt osqp_capabilities(void) {
-  return OSQP_CAPABILITY_INDIRECT_SOLVER | OSQP_CAPABILITY_UPDATE_MATRICES;
+  return OSQP_CAPABILITY_DIRECT_SOLVER | OSQP_CAPABILITY_INDIRECT_SOLVER | OSQP_CAPABILITY_UPDATE_MATRICES;
 }
 const char* osqp_version(void) { return "1.0.0-gb300"; }
 const char* osqp_error_message(OSQPInt e) {
@@ -504,7 +539,7 @@ OSQPCscMatrix* OSQPCscMatrix_identity(OSQPInt m) { return OSQPCscMatrix_diag_sca
 // --- validation (src/auxil.c:950-1223) -------------------------------------
 static int validate_settings(const OSQPSettings* s, int from_setup) {
   if (!s) return 1;
-  if (from_setup && s->linsys_solver != OSQP_INDIRECT_SOLVER) return 1;
+  if (from_setup && s->linsys_solver != OSQP_INDIRECT_SOLVER && s->linsys_solver != OSQP_DIRECT_SOLVER) return 1;
   if (from_setup && s->allocate_solution != 0 && s->allocate_solution != 1) return 1;
   if (s->verbose != 0 && s->verbose != 1) return 1;
   if (s->profiler_level < 0 || s->profiler_level > 2) return 1;
@@ -650,6 +685,36 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
     if (c1 < 1 || c2 < 1) w->cluster = (w->cluster > 8 && max_active_clusters(k_solve_cluster<T>, 8, kClusterThreads) > 0 &&
                                         max_active_clusters(k_setup_cluster<T>, 8, kClusterThreads) > 0) ? 8 : 1;
   }
+  // Direct solver: the plan on the host, then the CTA form with the
+  // factorisation and block solve in shared memory
+  KktPlan kplan;
+  const bool direct = settings->linsys_solver == OSQP_DIRECT_SOLVER;
+  if (direct) {
+    cudaFuncAttributes fa;
+    int optin = 0;
+    if (cudaFuncGetAttributes(&fa, k_solve_block<T>) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, w->device) != cudaSuccess) {
+      osqp_cleanup(solver); *solverp = NULL; return OSQP_ALGEBRA_LOAD_ERROR;
+    }
+    const long long room = (long long)optin - (long long)fa.sharedSizeBytes - 1024;
+    const int blim = kkt_bmax_limit(kBlockThreads, room, (int)sizeof(T));
+    const int prc = kkt_plan_build(n, m, Pp.data(), Pi.data(), Ap.data(), Ai.data(), blim, kplan);
+    const long long need = prc ? 0 : kkt_ws_bytes(n, kplan.bmax, kplan.nb, (int)sizeof(T));
+    if (prc || need > room) {
+      fprintf(stderr, "osqp_gb300: the direct KKT solver does not apply to this problem (n=%d, m=%d): %s\n", n, m,
+              prc == 1 ? "a block of its block-tridiagonal ordering exceeds the on-chip limit"
+              : prc ? "inconsistent structure" : "its solve vectors exceed the on-chip workspace");
+      osqp_cleanup(solver); *solverp = NULL; return OSQP_LINSYS_SOLVER_INIT_ERROR;
+    }
+    w->kdsm = (size_t)((need + 1023) & ~1023LL);
+    if (cudaFuncSetAttribute(k_solve_block<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)w->kdsm) != cudaSuccess ||
+        cudaFuncSetAttribute(k_setup_block<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)w->kdsm) != cudaSuccess ||
+        cudaFuncSetAttribute(k_refactor_block<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)w->kdsm) != cudaSuccess) {
+      osqp_cleanup(solver); *solverp = NULL; return OSQP_ALGEBRA_LOAD_ERROR;
+    }
+    w->use_grid = 0;
+    w->cluster = 1;
+  }
   if (w->use_grid) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve_grid<T>, kGridThreads, 0);
@@ -676,6 +741,10 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   size_t o_err = ap.take<int>(4);
   const int gb = w->use_grid ? w->grid_blocks : 1;
   size_t o_part = ap.take<double>((size_t)(4 * kMaxSum + 2 * kMaxMax) * gb);
+  const size_t knb1 = direct ? (size_t)kplan.nb + 1 : 0;
+  size_t o_kperm = ap.take<int>(direct ? n : 0), o_kiperm = ap.take<int>(direct ? n : 0);
+  size_t o_kbs = ap.take<int>(knb1), o_kfo = ap.take<int>(knb1), o_kco = ap.take<int>(knb1);
+  size_t o_kcr = ap.take<int>(direct ? kplan.cr.size() : 0), o_kF = ap.take<T>(direct ? (size_t)kplan.fsize : 0);
   w->arena_bytes = ap.off;
   if (cudaMalloc(&w->arena, w->arena_bytes) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_MEM_ALLOC_ERROR; }
   cudaMemsetAsync(w->arena, 0, w->arena_bytes, w->stream);
@@ -704,6 +773,21 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   w->err = (int*)(b + o_err);
   w->flag = w->err + 1;
   w->partials = (double*)(b + o_part);
+  if (direct) {
+    pr.kkt.nb = kplan.nb; pr.kkt.bmax = kplan.bmax;
+    pr.kkt.perm = (int*)(b + o_kperm); pr.kkt.iperm = (int*)(b + o_kiperm);
+    pr.kkt.bs = (int*)(b + o_kbs); pr.kkt.fo = (int*)(b + o_kfo); pr.kkt.co = (int*)(b + o_kco);
+    pr.kkt.cr = (int*)(b + o_kcr); pr.kkt.F = (T*)(b + o_kF);
+    cudaStream_t s0 = w->stream;
+    GB_TRY(cudaMemcpyAsync((void*)pr.kkt.perm, kplan.perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s0));
+    GB_TRY(cudaMemcpyAsync((void*)pr.kkt.iperm, kplan.iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s0));
+    GB_TRY(cudaMemcpyAsync((void*)pr.kkt.bs, kplan.bs.data(), sizeof(int) * knb1, cudaMemcpyHostToDevice, s0));
+    GB_TRY(cudaMemcpyAsync((void*)pr.kkt.fo, kplan.fo.data(), sizeof(int) * knb1, cudaMemcpyHostToDevice, s0));
+    GB_TRY(cudaMemcpyAsync((void*)pr.kkt.co, kplan.co.data(), sizeof(int) * knb1, cudaMemcpyHostToDevice, s0));
+    if (!kplan.cr.empty())
+      GB_TRY(cudaMemcpyAsync((void*)pr.kkt.cr, kplan.cr.data(), sizeof(int) * kplan.cr.size(), cudaMemcpyHostToDevice, s0));
+    GB_TRY(cudaStreamSynchronize(s0));   // the plan's host vectors end with this call
+  }
 
   // ---- raw data in (host or device pointers) ----
   cudaStream_t s = w->stream;
@@ -782,6 +866,13 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   if (cudaMallocHost((void**)&w->h_st, sizeof(SolverScalars)) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_MEM_ALLOC_ERROR; }
   int rc = launch_setup(w, 0);
   if (rc) { osqp_cleanup(solver); *solverp = NULL; return rc; }
+  if (direct) {
+    // the builtin's set-up reports a KKT matrix that is not quasi-definite
+    // (P not positive semidefinite) as OSQP_NONCVX_ERROR (osqp_api.c:500-505)
+    int fail = 0;
+    if (cudaMemcpy(&fail, &w->pr.st->kkt_fail, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) fail = -1;
+    if (fail) { osqp_cleanup(solver); *solverp = NULL; return fail > 0 ? OSQP_NONCVX_ERROR : OSQP_ALGEBRA_LOAD_ERROR; }
+  }
 
   if (settings->allocate_solution) {
     solver->solution = (OSQPSolution*)calloc(1, sizeof(OSQPSolution));
@@ -834,7 +925,7 @@ static int launch_setup(OSQPWorkspace* w, int keep_state) {
   } else if (w->cluster > 1) {
     GB_TRY(launch_clusters(k_setup_cluster<T>, 1, w->cluster, kClusterThreads, s, w->pr, w->ds, w->kktL, keep_state));
   } else {
-    k_setup_block<T><<<1, kBlockThreads, 0, s>>>(w->pr, w->ds, w->kktL, keep_state);
+    k_setup_block<T><<<1, kBlockThreads, w->kdsm, s>>>(w->pr, w->ds, w->kktL, keep_state);
     GB_TRY(cudaGetLastError());
   }
   return check_device_error(w);
@@ -855,7 +946,7 @@ static int launch_solve(OSQPWorkspace* w) {
   } else if (w->cluster > 1) {
     GB_TRY(launch_clusters(k_solve_cluster<T>, 1, w->cluster, kClusterThreads, s, w->pr, w->ds, w->kktL));
   } else {
-    k_solve_block<T><<<1, kBlockThreads, 0, s>>>(w->pr, w->ds, w->kktL);
+    k_solve_block<T><<<1, kBlockThreads, w->kdsm, s>>>(w->pr, w->ds, w->kktL);
     GB_TRY(cudaGetLastError());
   }
   cudaEventRecord(w->ev1, s);
@@ -976,6 +1067,12 @@ static const int kEwBlocks = 296, kEwThreads = 256;
 // Preconditioner refresh driven by the host: the Jacobi diagonal and, with
 // cg_precond = 2, the blocks of the block-Jacobi one.
 static void refresh_precond(OSQPWorkspace* w, cudaStream_t s, double rho, int rho_is_vec) {
+  if (w->pr.kkt.nb > 0) {
+    // direct solver: refactor for the rho in the device scalar state (and
+    // the rho vector, already refreshed on this stream)
+    k_refactor_block<T><<<1, kBlockThreads, w->kdsm, s>>>(w->pr, w->ds, w->kktL);
+    return;
+  }
   k_precond<T><<<kEwBlocks, kEwThreads, 0, s>>>(w->pr, w->ds.sigma, rho, rho_is_vec, w->ds.cg_precond);
   if (w->ds.cg_precond == kPrecondBlockDiagonal && w->pr.Binv)
     k_block_precond<T><<<block_precond_grid(w->n), kBlockPrecondThreads, 0, s>>>(w->pr, w->ds.sigma, rho, rho_is_vec);

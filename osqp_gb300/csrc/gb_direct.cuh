@@ -109,23 +109,33 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
       }
     }
     __syncthreads();
-    // ---- P entries, sigma, and rows of A with a single entry ----
-    for (int i = tid; i < b; i += nt) {
+    // ---- P entries, sigma, and rows of A with a single entry: one warp per
+    // variable (lanes over its entries; every P entry has its own target, the
+    // single-entry rows are summed in a fixed shuffle order) ----
+    for (int i = warp; i < b; i += nwarps) {
       const int v = kv.perm[s0 + i];
-      for (int e = P.rowptr[v]; e < P.rowptr[v + 1]; e++) {
+      const int pb0 = P.rowptr[v], pe0 = P.rowptr[v + 1];
+      for (int e = pb0 + lane; e < pe0; e += 32) {
         const int p = kv.iperm[P.col[e]];
         if (p >= sp && p < s0) Kc[i * bp + (p - sp)] += P.val[e];
-        else if (p >= s0 && p < e0) S[i * b + (p - s0)] += P.val[e];
+        else if (p >= s0 && p < e0 && p != s0 + i) S[i * b + (p - s0)] += P.val[e];
       }
-      T d = S[i * b + i] + sigma;
-      for (int e = At.rowptr[v]; e < At.rowptr[v + 1]; e++) {
+      T dsum = T(0), pdiag = T(0);
+      for (int e = pb0 + lane; e < pe0; e += 32)
+        if (P.col[e] == v) pdiag = P.val[e];
+      for (int e = At.rowptr[v] + lane; e < At.rowptr[v + 1]; e += 32) {
         const int row = At.col[e];
         if (A.rowptr[row + 1] - A.rowptr[row] == 1) {
           const T a = At.val[e];
-          d += (a * a) * (rho_vec ? rho_vec[row] : rho_s);
+          dsum += (a * a) * (rho_vec ? rho_vec[row] : rho_s);
         }
       }
-      S[i * b + i] = d;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        pdiag += __shfl_xor_sync(0xffffffffu, pdiag, o);   // one lane holds it
+      }
+      if (lane == 0) S[i * b + i] = ((S[i * b + i] + pdiag) + sigma) + dsum;
     }
     __syncthreads();
     T* Fk = kv.F + kv.fo[k];
@@ -195,6 +205,11 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
 // block, by sub-warps of kKktLanes lanes over threads [t0, t0 + tn); fn runs
 // on the sub-warp's first lane.  Loop bounds are uniform over each warp (t0
 // and tn multiples of 32).
+// Entries of a block row a lane loads before it multiplies (cols up to
+// kKktLanes x kKktRowChunk per round): the loads of a round are independent,
+// so a block row costs one memory latency per round, not one per entry.
+constexpr int kKktRowChunk = 8;
+
 template <typename T, typename FN>
 __device__ __forceinline__ void kkt_block_rows(const T* __restrict__ M, const T* v, int rows, int cols, int t0,
                                                int tn, FN fn) {
@@ -206,11 +221,32 @@ __device__ __forceinline__ void kkt_block_rows(const T* __restrict__ M, const T*
     T a = T(0);
     if (r < rows) {
       const T* Mr = M + (size_t)r * cols;
-      for (int j = sl; j < cols; j += kKktLanes) a += Mr[j] * v[j];
+      for (int j0 = sl; j0 < cols; j0 += kKktLanes * kKktRowChunk) {
+        T mv[kKktRowChunk];
+#pragma unroll
+        for (int u = 0; u < kKktRowChunk; u++) {
+          const int j = j0 + u * kKktLanes;
+          mv[u] = j < cols ? Mr[j] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kKktRowChunk; u++) {
+          const int j = j0 + u * kKktLanes;
+          if (j < cols) a += mv[u] * v[j];
+        }
+      }
     }
     a = subwarp_sum<kKktLanes>(a);
     if (r < rows && sl == 0) fn(r, a);
   }
+}
+
+// Copy the block starts and factor offsets (read at every block step) to
+// on-chip memory `dst` (2 (nb + 1) ints) and point kv at the copies.
+template <typename T>
+__device__ __forceinline__ void kkt_plan_on_chip(KktView<T>& kv, int* dst) {
+  for (int k = threadIdx.x; k <= kv.nb; k += blockDim.x) { dst[k] = kv.bs[k]; dst[kv.nb + 1 + k] = kv.fo[k]; }
+  kv.bs = dst;
+  kv.fo = dst + kv.nb + 1;
 }
 
 // Solve K x = b with the factor: c holds the permuted right-hand side on entry

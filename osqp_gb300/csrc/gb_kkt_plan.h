@@ -31,6 +31,12 @@
 #include <cstdlib>
 #include <vector>
 
+#if defined(__CUDACC__)
+#define GB_KKT_HD __host__ __device__
+#else
+#define GB_KKT_HD
+#endif
+
 namespace gb {
 
 // Constraint rows gathered per assembly pass of a block, and the largest
@@ -43,14 +49,19 @@ constexpr int kKktMergeTo = 32;
 
 // On-chip workspace of the block factorisation (elements): S_{k-1}^-1, S_k,
 // its sweep buffer, K_{k,k-1}, G_k, the assembly tile and its rho values.
-inline long long kkt_factor_ws_elems(int bmax) {
+GB_KKT_HD inline long long kkt_factor_ws_elems(int bmax) {
   return 5LL * bmax * bmax + (long long)kKktTileRows * 2 * bmax + kKktTileRows;
 }
 // Whole on-chip workspace of a direct solve: the factorisation's, or the two
 // permuted n-vectors of the block-tridiagonal solve, whichever is larger.
-inline long long kkt_ws_elems(int n, int bmax) {
+GB_KKT_HD inline long long kkt_ws_elems(int n, int bmax) {
   const long long f = kkt_factor_ws_elems(bmax), v = 2LL * n;
   return ((f > v ? f : v) + 3) & ~3LL;
+}
+// Bytes of the whole workspace: the elements above, then copies of the block
+// starts and factor offsets (2 (nb + 1) ints) that every block step reads.
+GB_KKT_HD inline long long kkt_ws_bytes(int n, int bmax, int nb, int elem) {
+  return kkt_ws_elems(n, bmax) * elem + 8LL * (nb + 1);
 }
 
 struct KktPlan {

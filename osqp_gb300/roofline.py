@@ -16,6 +16,13 @@ generic CSR; every vector operand counted once per use (ideal reuse).
   block-Jacobi preconditioner (cg_precond = 2): the PCG iteration reads the
       32 x 32 blocks of M^-1, ceil(n / 32) * 1024 * w bytes, instead of the
       n*w diagonal
+  direct solver (block-tridiagonal factor of F elements, gb_direct.cuh):
+      ADMM iteration  B(A') + B(A) + F*w [one forward and one backward sweep
+                      read each factor block once] + 2*n*4 [permutation]
+                      + 10*n*w + 12*m*w
+      factorisation   (set-up and every rho update) F*w written
+                      + B(P_full) + 2*B(A) + B(A') read (every row of A
+                      touches at most two blocks)
 """
 from __future__ import annotations
 
@@ -53,3 +60,15 @@ def pfull_nnz(P_triu) -> int:
     has_diag[coo.row[coo.row == coo.col]] = True
     nd = int(has_diag.sum())
     return 2 * P.nnz - 2 * nd + n
+
+
+def direct_solve_bytes(n, m, nnz_pfull, nnz_a, w, admm_iters, factor_elems, factorisations, check_termination):
+    """Algorithmic bytes of one direct-solver QP solve (see the module docstring)."""
+    bp = spmv_bytes(n, n, nnz_pfull, w)
+    ba = spmv_bytes(m, n, nnz_a, w)
+    bat = spmv_bytes(n, m, nnz_a, w)
+    it = bat + ba + factor_elems * w + 2 * n * 4 + 10 * n * w + 12 * m * w
+    term = bp + ba + bat + 8 * (n + m) * w
+    fac = factor_elems * w + bp + 2 * ba + bat
+    checks = admm_iters // max(1, check_termination) + 1
+    return admm_iters * it + checks * term + factorisations * fac
