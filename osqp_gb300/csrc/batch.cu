@@ -73,6 +73,7 @@ struct BatchInst {
   // direct KKT solve (knb == 0: the PCG): blocks, largest block, offsets of
   // the QP's block lists, constraint lists and factor
   int knb, kbmax, kb_off, kcr_off;
+  int kring, ksegmax;   // bulk-copy ring slots of the solve and largest factor segment
   long long kf_off;
 };
 
@@ -89,7 +90,7 @@ struct BatchArrays {
   const BatchInst* inst;
   TT* Binv;             // block-Jacobi blocks of every QP (nullptr unless cg_precond = 2)
   // direct KKT solve: plans and factors of every QP (gb_kkt_plan.h)
-  int *kperm, *kiperm, *kbs, *kfo, *kco, *kcr;
+  int *kperm, *kiperm, *kbs, *kfo, *kbo, *kco, *kcr;
   TT* kF;
 
   __device__ DevProblem<TT> problem(int k) const {
@@ -117,7 +118,9 @@ struct BatchArrays {
     pr.Arow_g = pr.A.rowptr; pr.Acol_g = Acol; pr.Aval_g = Aval;
     if (b.knb > 0) {
       pr.kkt.nb = b.knb; pr.kkt.bmax = b.kbmax;
-      pr.kkt.bs = kbs + b.kb_off; pr.kkt.fo = kfo + b.kb_off; pr.kkt.co = kco + b.kb_off;
+      pr.kkt.ring = b.kring; pr.kkt.segmax = b.ksegmax;
+      pr.kkt.bs = kbs + b.kb_off; pr.kkt.fo = kfo + b.kb_off; pr.kkt.bo = kbo + b.kb_off;
+      pr.kkt.co = kco + b.kb_off;
       pr.kkt.cr = kcr + b.kcr_off;
       pr.kkt.perm = kperm + o; pr.kkt.iperm = kiperm + o;
       pr.kkt.F = kF + b.kf_off;
@@ -298,7 +301,7 @@ __device__ Spans cluster_spans(const DevProblem<TT>& pr, int kktL, int r, int c,
 template <typename TT, typename G>
 __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s, int k, int mode,
                            GroupShared& gsh, SolverScalars& ssc, unsigned char* dsm, int dsm_bytes,
-                           int it_lo, int it_hi, int stage_mat) {
+                           int it_lo, int it_hi, int stage_mat, KktPipe* kpipe = nullptr) {
   DevProblem<TT> pv = B.problem(k);
   if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; if (mode != kModeSetup) ssc = *pv.st; }
   __syncthreads();
@@ -308,7 +311,9 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   const bool direct = pv.kkt.nb > 0;
   if (direct) {
     pv.kws = (TT*)dsm;
-    kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.kkt.bmax) * sizeof(TT)));
+    pv.kpipe = kpipe;
+    if (!kpipe) pv.kkt.ring = 0;
+    kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.kkt.bmax, pv.kkt.segmax, pv.kkt.ring) * sizeof(TT)));
     __syncthreads();
   }
   if (mode == kModeSolve && dsm_bytes > 0 && !direct) {
@@ -387,7 +392,9 @@ k_batch(BatchArrays<TT> B, DevSettings s, BatchLaunch L) {
   __shared__ GroupShared gsh;
   __shared__ SolverScalars ssc;
   __shared__ int s_idx;
+  __shared__ KktPipe kpipe;
   BlockGroup g{&gsh};
+  kkt_pipe_init(&kpipe);
   const int count = L.count_dev ? *L.count_dev : L.count;
   for (;;) {
     if (threadIdx.x == 0) s_idx = atomicAdd(L.queue, 1);
@@ -396,7 +403,7 @@ k_batch(BatchArrays<TT> B, DevSettings s, BatchLaunch L) {
     __syncthreads();
     if (idx >= count) break;
     batch_item(g, B, s, L.order[idx], L.mode, gsh, ssc, g_batch_dsm, L.dsm_bytes, L.it_lo, L.it_hi,
-               L.stage_mat);
+               L.stage_mat, &kpipe);
     if (threadIdx.x == 0) *B.problem(L.order[idx]).st = ssc;
     __syncthreads();
   }
@@ -869,7 +876,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     std::vector<OSQPInt> hAi(ao > 0 ? ao : 1);
     if (ao && cudaMemcpy(hAi.data(), Ai, sizeof(OSQPInt) * ao, cudaMemcpyDefault) != cudaSuccess) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
     plans.resize(count);
-    std::vector<int> prc(count, 0);
+    std::vector<int> prc(count, 0), ring(count, 0);
     const int nthr = std::max(1, std::min((int)std::thread::hardware_concurrency(), std::min(count, 64)));
     std::vector<std::thread> pool;
     for (int t = 0; t < nthr; t++)
@@ -878,7 +885,14 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
           const BatchInst& I = b->inst[k];
           prc[k] = kkt_plan_build(I.n, I.m, hPp.data() + pp_off[k], hPi.data() + I.pt_off, hAp.data() + pp_off[k],
                                   hAi.data() + I.a_off, blim, plans[k]);
-          if (!prc[k] && kkt_ws_bytes(I.n, plans[k].bmax, plans[k].nb, (int)sizeof(T)) > b->dsm) prc[k] = 3;
+          if (!prc[k]) {
+            // ring slots of the solve's bulk-copy pipeline: as many as fit (at least 2), else none
+            int R = kKktRingMax;
+            while (R >= 2 && kkt_ws_bytes(I.n, plans[k].bmax, plans[k].nb, plans[k].segmax, R, (int)sizeof(T)) > b->dsm) R--;
+            if (R < 2) R = 0;
+            if (kkt_ws_bytes(I.n, plans[k].bmax, plans[k].nb, plans[k].segmax, R, (int)sizeof(T)) > b->dsm) prc[k] = 3;
+            ring[k] = R;
+          }
         }
       });
     for (auto& th : pool) th.join();
@@ -893,13 +907,17 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
       }
       BatchInst& I = b->inst[k];
       I.knb = plans[k].nb; I.kbmax = plans[k].bmax;
+      I.kring = env_int("OSQP_GB300_KKT_RING", 1) ? ring[k] : 0; I.ksegmax = plans[k].segmax;
       I.kb_off = (int)kb_tot; I.kcr_off = (int)kcr_tot; I.kf_off = kf_tot;
       kb_tot += plans[k].nb + 1; kcr_tot += (long long)plans[k].cr.size(); kf_tot += plans[k].fsize;
     }
     if (kb_tot > INT32_MAX || kcr_tot > INT32_MAX) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
     b->kf_total = kf_tot;
   } else {
-    for (int k = 0; k < count; k++) { BatchInst& I = b->inst[k]; I.knb = 0; I.kbmax = 0; I.kb_off = 0; I.kcr_off = 0; I.kf_off = 0; }
+    for (int k = 0; k < count; k++) {
+      BatchInst& I = b->inst[k];
+      I.knb = 0; I.kbmax = 0; I.kb_off = 0; I.kcr_off = 0; I.kf_off = 0; I.kring = 0; I.ksegmax = 0;
+    }
   }
 
   // ---- arena ----
@@ -926,6 +944,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   size_t o_binv = pl.take(sizeof(T) * b->binv_elems);
   size_t o_kperm = pl.take(sizeof(int) * (b->direct ? nsum : 0)), o_kiperm = pl.take(sizeof(int) * (b->direct ? nsum : 0));
   size_t o_kbs = pl.take(sizeof(int) * kb_tot), o_kfo = pl.take(sizeof(int) * kb_tot), o_kco = pl.take(sizeof(int) * kb_tot);
+  size_t o_kbo = pl.take(sizeof(int) * kb_tot);
   size_t o_kcr = pl.take(sizeof(int) * kcr_tot), o_kF = pl.take(sizeof(T) * kf_tot);
   {
     // admission by free device memory: refuse (rather than fail part-way)
@@ -952,6 +971,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   B.Binv = b->binv_elems ? (T*)(a + o_binv) : nullptr;
   B.kperm = (int*)(a + o_kperm); B.kiperm = (int*)(a + o_kiperm);
   B.kbs = (int*)(a + o_kbs); B.kfo = (int*)(a + o_kfo); B.kco = (int*)(a + o_kco); B.kcr = (int*)(a + o_kcr);
+  B.kbo = (int*)(a + o_kbo);
   B.kF = (T*)(a + o_kF);
   b->d_inst = (BatchInst*)(a + o_inst); B.inst = b->d_inst;
   b->d_order = (int*)(a + o_order);
@@ -972,7 +992,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     BT_TRY(cudaMemcpyAsync(B.vm[3], u, sizeof(T) * msum, cudaMemcpyDefault, s));
   }
   BT_TRY(cudaMemcpyAsync(B.Atcol, Ai, sizeof(int) * ao, cudaMemcpyDefault, s));
-  std::vector<int> kperm_h, kiperm_h, kbs_h, kfo_h, kco_h, kcr_h;
+  std::vector<int> kperm_h, kiperm_h, kbs_h, kfo_h, kbo_h, kco_h, kcr_h;
   if (b->direct) {
     kperm_h.reserve(nsum); kiperm_h.reserve(nsum); kbs_h.reserve(kb_tot); kfo_h.reserve(kb_tot); kco_h.reserve(kb_tot);
     kcr_h.reserve(kcr_tot);
@@ -982,6 +1002,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
       kiperm_h.insert(kiperm_h.end(), q.iperm.begin(), q.iperm.end());
       kbs_h.insert(kbs_h.end(), q.bs.begin(), q.bs.end());
       kfo_h.insert(kfo_h.end(), q.fo.begin(), q.fo.end());
+      kbo_h.insert(kbo_h.end(), q.bo.begin(), q.bo.end());
       kco_h.insert(kco_h.end(), q.co.begin(), q.co.end());
       kcr_h.insert(kcr_h.end(), q.cr.begin(), q.cr.end());
     }
@@ -989,6 +1010,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     BT_TRY(cudaMemcpyAsync(B.kiperm, kiperm_h.data(), sizeof(int) * nsum, cudaMemcpyHostToDevice, s));
     BT_TRY(cudaMemcpyAsync(B.kbs, kbs_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
     BT_TRY(cudaMemcpyAsync(B.kfo, kfo_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
+    BT_TRY(cudaMemcpyAsync(B.kbo, kbo_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
     BT_TRY(cudaMemcpyAsync(B.kco, kco_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
     if (kcr_tot) BT_TRY(cudaMemcpyAsync(B.kcr, kcr_h.data(), sizeof(int) * kcr_tot, cudaMemcpyHostToDevice, s));
     plans.clear();

@@ -65,10 +65,12 @@ constexpr int kGridThreads = 1024;
 extern __shared__ __align__(16) unsigned char g_engine_dsm[];
 
 template <typename TT>
-__device__ __forceinline__ void attach_direct_ws(DevProblem<TT>& pr) {
+__device__ __forceinline__ void attach_direct_ws(DevProblem<TT>& pr, KktPipe* kpipe = nullptr) {
   if (pr.kkt.nb > 0) {
     pr.kws = (TT*)g_engine_dsm;
-    kkt_plan_on_chip(pr.kkt, (int*)(g_engine_dsm + kkt_ws_elems(pr.n, pr.kkt.bmax) * sizeof(TT)));
+    pr.kpipe = kpipe;
+    if (!kpipe) pr.kkt.ring = 0;
+    kkt_plan_on_chip(pr.kkt, (int*)(g_engine_dsm + kkt_ws_elems(pr.n, pr.kkt.bmax, pr.kkt.segmax, pr.kkt.ring) * sizeof(TT)));
     __syncthreads();
   }
 }
@@ -93,8 +95,10 @@ __global__ void __launch_bounds__(kBlockThreads, 1)
 k_solve_block(DevProblem<TT> pr, DevSettings s, int kktL) {
   __shared__ GroupShared gsh;
   __shared__ SolverScalars ssc;
+  __shared__ KktPipe kpipe;
   if (threadIdx.x == 0) { gsh.parity = 0; gsh.flag = 0; ssc = *pr.st; }
-  attach_direct_ws(pr);
+  kkt_pipe_init(&kpipe);
+  attach_direct_ws(pr, &kpipe);
   __syncthreads();
   BlockGroup g{&gsh};
   Solver<TT> S{pr, s, &ssc, kktL};
@@ -688,6 +692,7 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   // Direct solver: the plan on the host, then the CTA form with the
   // factorisation and block solve in shared memory
   KktPlan kplan;
+  int kring = 0;
   const bool direct = settings->linsys_solver == OSQP_DIRECT_SOLVER;
   if (direct) {
     cudaFuncAttributes fa;
@@ -699,7 +704,11 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
     const long long room = (long long)optin - (long long)fa.sharedSizeBytes - 1024;
     const int blim = kkt_bmax_limit(kBlockThreads, room, (int)sizeof(T));
     const int prc = kkt_plan_build(n, m, Pp.data(), Pi.data(), Ap.data(), Ai.data(), blim, kplan);
-    const long long need = prc ? 0 : kkt_ws_bytes(n, kplan.bmax, kplan.nb, (int)sizeof(T));
+    int R = kKktRingMax;
+    while (!prc && R >= 2 && kkt_ws_bytes(n, kplan.bmax, kplan.nb, kplan.segmax, R, (int)sizeof(T)) > room) R--;
+    if (R < 2) R = 0;
+    const long long need = prc ? 0 : kkt_ws_bytes(n, kplan.bmax, kplan.nb, kplan.segmax, R, (int)sizeof(T));
+    kring = R;
     if (prc || need > room) {
       fprintf(stderr, "osqp_gb300: the direct KKT solver does not apply to this problem (n=%d, m=%d): %s\n", n, m,
               prc == 1 ? "a block of its block-tridiagonal ordering exceeds the on-chip limit"
@@ -743,7 +752,7 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   size_t o_part = ap.take<double>((size_t)(4 * kMaxSum + 2 * kMaxMax) * gb);
   const size_t knb1 = direct ? (size_t)kplan.nb + 1 : 0;
   size_t o_kperm = ap.take<int>(direct ? n : 0), o_kiperm = ap.take<int>(direct ? n : 0);
-  size_t o_kbs = ap.take<int>(knb1), o_kfo = ap.take<int>(knb1), o_kco = ap.take<int>(knb1);
+  size_t o_kbs = ap.take<int>(knb1), o_kfo = ap.take<int>(knb1), o_kco = ap.take<int>(knb1), o_kbo = ap.take<int>(knb1);
   size_t o_kcr = ap.take<int>(direct ? kplan.cr.size() : 0), o_kF = ap.take<T>(direct ? (size_t)kplan.fsize : 0);
   w->arena_bytes = ap.off;
   if (cudaMalloc(&w->arena, w->arena_bytes) != cudaSuccess) { osqp_cleanup(solver); *solverp = NULL; return OSQP_MEM_ALLOC_ERROR; }
@@ -775,6 +784,8 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
   w->partials = (double*)(b + o_part);
   if (direct) {
     pr.kkt.nb = kplan.nb; pr.kkt.bmax = kplan.bmax;
+    pr.kkt.ring = kring; pr.kkt.segmax = kplan.segmax;
+    pr.kkt.bo = (int*)(b + o_kbo);
     pr.kkt.perm = (int*)(b + o_kperm); pr.kkt.iperm = (int*)(b + o_kiperm);
     pr.kkt.bs = (int*)(b + o_kbs); pr.kkt.fo = (int*)(b + o_kfo); pr.kkt.co = (int*)(b + o_kco);
     pr.kkt.cr = (int*)(b + o_kcr); pr.kkt.F = (T*)(b + o_kF);
@@ -783,6 +794,7 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
     GB_TRY(cudaMemcpyAsync((void*)pr.kkt.iperm, kplan.iperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s0));
     GB_TRY(cudaMemcpyAsync((void*)pr.kkt.bs, kplan.bs.data(), sizeof(int) * knb1, cudaMemcpyHostToDevice, s0));
     GB_TRY(cudaMemcpyAsync((void*)pr.kkt.fo, kplan.fo.data(), sizeof(int) * knb1, cudaMemcpyHostToDevice, s0));
+    GB_TRY(cudaMemcpyAsync((void*)pr.kkt.bo, kplan.bo.data(), sizeof(int) * knb1, cudaMemcpyHostToDevice, s0));
     GB_TRY(cudaMemcpyAsync((void*)pr.kkt.co, kplan.co.data(), sizeof(int) * knb1, cudaMemcpyHostToDevice, s0));
     if (!kplan.cr.empty())
       GB_TRY(cudaMemcpyAsync((void*)pr.kkt.cr, kplan.cr.data(), sizeof(int) * kplan.cr.size(), cudaMemcpyHostToDevice, s0));

@@ -16,6 +16,14 @@
 // reduced form of the builtin's solve (qdldl_interface.c:431-466 gives the
 // same x~ and z~ in exact arithmetic).
 //
+// The solve streams the factor through shared memory: each block's segment
+// (gb_kkt_plan.h) is one bulk copy (cp.async.bulk, the TMA engine's untiled
+// form) into a ring of `ring` slots, issued by one thread several segments
+// ahead of use and tracked by one mbarrier per slot, so the dependent chain of
+// block steps reads only shared memory.  Waits are bounded: a copy that does
+// not arrive within the limit makes the solve read that segment from global
+// memory instead (and records it in the pipe's error word).
+//
 // Everything is deterministic: each entry has one owner thread and a fixed
 // summation order, so a QP's factor and solutions do not depend on the rest
 // of a batch.  A pivot that is not positive and finite means K is not
@@ -34,8 +42,10 @@ constexpr int kKktLanes = 8;
 template <typename T>
 struct KktView {
   int nb = 0, bmax = 0;          // nb == 0: no direct solve
+  int ring = 0, segmax = 0;      // bulk-copy ring slots of the solve (0: no ring), largest segment
   const int* bs = nullptr;       // [nb + 1]
-  const int* fo = nullptr;       // [nb + 1]
+  const int* fo = nullptr;       // [nb + 1] forward segments
+  const int* bo = nullptr;       // [nb + 1] backward segments
   const int* co = nullptr;       // [nb + 1] (positions in cr)
   const int* cr = nullptr;
   const int* perm = nullptr;     // permuted position -> variable
@@ -138,7 +148,8 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
       if (lane == 0) S[i * b + i] = ((S[i * b + i] + pdiag) + sigma) + dsum;
     }
     __syncthreads();
-    T* Fk = kv.F + kv.fo[k];
+    T* Fk = kv.F + kv.fo[k];                         // forward segment: G_k, then S_k^-1
+    T* Sg = Fk + kkt_pad4((long long)b * bp);
     if (k > 0) {
       // ---- G_k = K_{k,k-1} S_{k-1}^-1 ; S_k -= G_k K_{k,k-1}' (lower
       // triangle, mirrored: S_k stays exactly symmetric) ----
@@ -158,8 +169,8 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
         S[i * b + j] = v;
         S[j * b + i] = v;
       }
-      T* Gg = Fk + b * b;
-      T* GTg = Gg + b * bp;
+      T* Gg = Fk;
+      T* GTg = kv.F + kv.bo[k];
       for (int o = tid; o < b * bp; o += nt) {
         Gg[o] = G[o];
         const int j = o / b, i = o - j * b;   // G' is bp x b
@@ -193,11 +204,14 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
     }
     for (int o = tid; o < b * b; o += nt) {
       const T v = -src[o];
-      Fk[o] = v;
+      Sg[o] = v;
       Sprev[o] = v;
     }
     __syncthreads();
   }
+  // the solve reads the factor through the async (bulk-copy) proxy
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+  __syncthreads();
   return true;
 }
 
@@ -240,13 +254,155 @@ __device__ __forceinline__ void kkt_block_rows(const T* __restrict__ M, const T*
   }
 }
 
-// Copy the block starts and factor offsets (read at every block step) to
-// on-chip memory `dst` (2 (nb + 1) ints) and point kv at the copies.
+// Copy the block starts and segment offsets (read at every block step) to
+// on-chip memory `dst` (3 (nb + 1) ints) and point kv at the copies.
 template <typename T>
 __device__ __forceinline__ void kkt_plan_on_chip(KktView<T>& kv, int* dst) {
-  for (int k = threadIdx.x; k <= kv.nb; k += blockDim.x) { dst[k] = kv.bs[k]; dst[kv.nb + 1 + k] = kv.fo[k]; }
+  const int w = kv.nb + 1;
+  for (int k = threadIdx.x; k < w; k += blockDim.x) { dst[k] = kv.bs[k]; dst[w + k] = kv.fo[k]; dst[2 * w + k] = kv.bo[k]; }
   kv.bs = dst;
-  kv.fo = dst + kv.nb + 1;
+  kv.fo = dst + w;
+  kv.bo = dst + 2 * w;
+}
+
+// ---------------------------------------------------------------------------
+// Bulk-copy pipeline state of a CTA: one mbarrier per ring slot and the number
+// of copies issued so far (copy Q goes to slot Q % ring; its wait parity is
+// (Q / ring) & 1).  Lives in static shared memory; kkt_pipe_init once per
+// kernel before the first solve.
+// ---------------------------------------------------------------------------
+struct KktPipe {
+  unsigned long long bar[kKktRingMax];
+  unsigned q;
+  int err;
+};
+
+__device__ __forceinline__ unsigned kkt_smem(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void kkt_pipe_init(KktPipe* pp) {
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kKktRingMax; s++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(kkt_smem(&pp->bar[s])) : "memory");
+    pp->q = 0;
+    pp->err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+// Wait (bounded: about 50 ms of device time) for the phase of the given
+// parity of an mbarrier.
+constexpr unsigned long long kKktWaitNs = 50ull * 1000 * 1000;
+__device__ __forceinline__ bool kkt_wait(unsigned long long* bar, unsigned parity) {
+  const unsigned a = kkt_smem(bar);
+  unsigned long long t0 = 0;
+  for (unsigned i = 0;; i++) {
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                 " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+    if (ok) return true;
+    if ((i & 31u) == 31u) {
+      const unsigned long long t = global_ns();
+      if (!t0) t0 = t;
+      else if (t - t0 > kKktWaitNs) return false;
+    }
+  }
+}
+
+// One bulk copy global -> shared of `bytes` (multiple of 16, both addresses
+// 16-byte aligned), completing a transaction on `bar`.  One thread.
+__device__ __forceinline__ void kkt_bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(kkt_smem(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               :: "r"(kkt_smem(dst)), "l"(src), "r"(bytes), "r"(kkt_smem(bar)) : "memory");
+}
+
+// The solve of kkt_solve with the factor streamed through `ring` (kv.ring
+// slots of kv.segmax elements).  Copies j = 0..nb-1 are the forward segments,
+// j = nb + t the backward segment of block nb - 1 - t.  A step may refill the
+// slot of a copy no later step needs; at most kv.ring copies are ahead.
+template <typename T, typename XO>
+__device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T* ring, XO xout) {
+  const int nt = blockDim.x, half = nt >> 1;
+  const bool lo = (int)threadIdx.x < half;
+  const int nb = kv.nb, R = kv.ring, SM = kv.segmax;
+  const unsigned q0 = pp->q;
+  const int total = 2 * nb - 1;
+  int issued = 0;                                     // thread 0's count
+  auto seg = [&](int j, long long& elems) -> const T* {
+    if (j < nb) {
+      const long long b = kv.bs[j + 1] - kv.bs[j], bp = j ? kv.bs[j] - kv.bs[j - 1] : 0;
+      elems = kkt_pad4(b * bp) + kkt_pad4(b * b);
+      return kv.F + kv.fo[j];
+    }
+    const int k = nb - 1 - (j - nb);
+    const long long b = kv.bs[k + 1] - kv.bs[k], bp = kv.bs[k] - kv.bs[k - 1];
+    elems = kkt_pad4(b * bp);
+    return kv.F + kv.bo[k];
+  };
+  auto slot = [&](int j) { return ring + (size_t)((q0 + (unsigned)j) % (unsigned)R) * SM; };
+  auto issue_upto = [&](int lim) {
+    if (threadIdx.x == 0) {
+      const int end = lim < total ? lim : total;
+      for (; issued < end; issued++) {
+        long long el;
+        const T* g = seg(issued, el);
+        kkt_bulk_load(slot(issued), g, (unsigned)(el * sizeof(T)), &pp->bar[(q0 + (unsigned)issued) % (unsigned)R]);
+      }
+    }
+  };
+  // pointer to copy j's data: the ring slot, or global memory after a failed wait
+  // (after one failed wait the CTA stops waiting and reads global memory)
+  auto get = [&](int j) -> const T* {
+    const unsigned Q = q0 + (unsigned)j;
+    long long el;
+    if (*(volatile int*)&pp->err) return seg(j, el);
+    if (!kkt_wait(&pp->bar[Q % (unsigned)R], (Q / (unsigned)R) & 1u)) {
+      *(volatile int*)&pp->err = 1;
+      return seg(j, el);
+    }
+    return slot(j);
+  };
+  issue_upto(R);
+  const T* cur = get(0);
+  for (int k = 1; k < nb; k++) {
+    const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+    const int spp = k > 1 ? kv.bs[k - 2] : sp;
+    issue_upto(k - 1 + R);            // copies < k - 1 are no longer needed
+    const T* prev = cur;              // segment k - 1: S_{k-1}^-1 after G_{k-1}
+    cur = get(k);                     // segment k: G_k first
+    if (lo) {
+      kkt_block_rows(cur, c + sp, b, bp, 0, half, [&](int r, T a) { c[s0 + r] -= a; });
+    } else {
+      const T* Si = prev + kkt_pad4((long long)bp * (sp - spp));
+      kkt_block_rows(Si, c + sp, bp, bp, half, nt - half, [&](int r, T a) { d[sp + r] = a; });
+    }
+    __syncthreads();
+  }
+  {
+    const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
+    const int bp = nb > 1 ? s0 - kv.bs[nb - 2] : 0;
+    issue_upto(nb - 1 + R);
+    const T* Si = cur + kkt_pad4((long long)b * bp);
+    kkt_block_rows(Si, c + s0, b, b, 0, nt, [&](int r, T a) { d[s0 + r] = a; });
+    __syncthreads();
+  }
+  for (int t = 0; t + 1 < nb; t++) {
+    const int k = nb - 1 - t;
+    const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+    issue_upto(nb + t + R);           // copies < nb + t are no longer needed
+    const T* GT = get(nb + t);
+    if (lo) {
+      kkt_block_rows(GT, d + s0, bp, b, 0, half, [&](int r, T a) { d[sp + r] -= a; });
+    } else {
+      for (int r = threadIdx.x - half; r < b; r += nt - half) xout(kv.perm[s0 + r], d[s0 + r]);
+    }
+    __syncthreads();
+  }
+  for (int r = threadIdx.x; r < kv.bs[1]; r += nt) xout(kv.perm[r], d[r]);
+  if (threadIdx.x == 0) pp->q = q0 + (unsigned)total;
+  __syncthreads();
 }
 
 // Solve K x = b with the factor: c holds the permuted right-hand side on entry
@@ -261,25 +417,28 @@ __device__ void kkt_solve(const KktView<T>& kv, T* c, T* d, XO xout) {
   // forward: c_k -= G_k c_{k-1} (lower half) while d_{k-1} = S_{k-1}^-1 c_{k-1} (upper half)
   for (int k = 1; k < nb; k++) {
     const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+    const int spp = k > 1 ? kv.bs[k - 2] : sp;
     if (lo) {
-      const T* G = kv.F + kv.fo[k] + b * b;
+      const T* G = kv.F + kv.fo[k];
       kkt_block_rows(G, c + sp, b, bp, 0, half, [&](int r, T a) { c[s0 + r] -= a; });
     } else {
-      const T* Si = kv.F + kv.fo[k - 1];
+      const T* Si = kv.F + kv.fo[k - 1] + kkt_pad4((long long)bp * (sp - spp));
       kkt_block_rows(Si, c + sp, bp, bp, half, nt - half, [&](int r, T a) { d[sp + r] = a; });
     }
     __syncthreads();
   }
   {
     const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
-    kkt_block_rows(kv.F + kv.fo[nb - 1], c + s0, b, b, 0, nt, [&](int r, T a) { d[s0 + r] = a; });
+    const int bp = nb > 1 ? s0 - kv.bs[nb - 2] : 0;
+    kkt_block_rows(kv.F + kv.fo[nb - 1] + kkt_pad4((long long)b * bp), c + s0, b, b, 0, nt,
+                   [&](int r, T a) { d[s0 + r] = a; });
     __syncthreads();
   }
   // backward: x_{k-1} = d_{k-1} - G_k' x_k (lower half) while block k is written out (upper half)
   for (int k = nb - 1; k >= 1; k--) {
     const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
     if (lo) {
-      const T* GT = kv.F + kv.fo[k] + b * b + b * bp;
+      const T* GT = kv.F + kv.bo[k];
       kkt_block_rows(GT, d + s0, bp, b, 0, half, [&](int r, T a) { d[sp + r] -= a; });
     } else {
       for (int r = threadIdx.x - half; r < b; r += nt - half) xout(kv.perm[s0 + r], d[s0 + r]);

@@ -20,10 +20,14 @@
 // the blocks are the stages (x_k, u_k), so the factor costs
 // O(T (nx + nu)^3) and each solve O(T (nx + nu)^2).
 //
-// Storage of the factor (elements of OSQPFloat), block k of size b_k after
-// the previous block of size b_{k-1}:
-//   [ S_k^-1 (b_k x b_k) | G_k (b_k x b_{k-1}) | G_k' (b_{k-1} x b_k) ]
+// Storage of the factor (elements of OSQPFloat; every segment padded to a
+// multiple of 4 elements, so each starts on a 16-byte boundary and can be
+// fetched by one bulk copy), block k of size b_k after one of size b_{k-1}:
+//   forward segment k   [ G_k (b_k x b_{k-1}) | S_k^-1 (b_k x b_k) ]   at fo[k]
+//   backward segment k  [ G_k' (b_{k-1} x b_k) ]                        at bo[k]
 // with G_k = K_{k,k-1} S_{k-1}^-1 and S_k = K_kk - G_k K_{k,k-1}' (block LDL').
+// The forward sweep of a solve reads the forward segments in order, the
+// backward sweep the backward segments in reverse order.
 #pragma once
 
 #include <algorithm>
@@ -47,21 +51,29 @@ constexpr int kKktOutMax = 24;
 // Blocks are merged while the merged block stays at or below this size.
 constexpr int kKktMergeTo = 32;
 
+// Factor segments hold multiples of 4 elements.
+GB_KKT_HD inline long long kkt_pad4(long long e) { return (e + 3) & ~3LL; }
+// Ring slots of the solve's bulk-copy pipeline (0: the solve reads the factor
+// from global memory directly).
+constexpr int kKktRingMax = 4;
+
 // On-chip workspace of the block factorisation (elements): S_{k-1}^-1, S_k,
 // its sweep buffer, K_{k,k-1}, G_k, the assembly tile and its rho values.
 GB_KKT_HD inline long long kkt_factor_ws_elems(int bmax) {
   return 5LL * bmax * bmax + (long long)kKktTileRows * 2 * bmax + kKktTileRows;
 }
-// Whole on-chip workspace of a direct solve: the factorisation's, or the two
-// permuted n-vectors of the block-tridiagonal solve, whichever is larger.
-GB_KKT_HD inline long long kkt_ws_elems(int n, int bmax) {
-  const long long f = kkt_factor_ws_elems(bmax), v = 2LL * n;
-  return ((f > v ? f : v) + 3) & ~3LL;
+// Whole on-chip workspace of a direct solve: the factorisation's, or the
+// solve's (two permuted n-vectors and `ring` slots of segmax elements),
+// whichever is larger.
+GB_KKT_HD inline long long kkt_ws_elems(int n, int bmax, int segmax, int ring) {
+  const long long f = kkt_factor_ws_elems(bmax), v = kkt_pad4(2LL * n) + (long long)ring * segmax;
+  return kkt_pad4(f > v ? f : v);
 }
 // Bytes of the whole workspace: the elements above, then copies of the block
-// starts and factor offsets (2 (nb + 1) ints) that every block step reads.
-GB_KKT_HD inline long long kkt_ws_bytes(int n, int bmax, int nb, int elem) {
-  return kkt_ws_elems(n, bmax) * elem + 8LL * (nb + 1);
+// starts and the forward / backward segment offsets (3 (nb + 1) ints) that
+// every block step reads.
+GB_KKT_HD inline long long kkt_ws_bytes(int n, int bmax, int nb, int segmax, int ring, int elem) {
+  return kkt_ws_elems(n, bmax, segmax, ring) * elem + 12LL * (nb + 1);
 }
 
 struct KktPlan {
@@ -69,7 +81,9 @@ struct KktPlan {
   std::vector<int> perm;    // permuted position -> variable
   std::vector<int> iperm;   // variable -> permuted position
   std::vector<int> bs;      // [nb + 1] block starts (permuted positions)
-  std::vector<int> fo;      // [nb + 1] factor offsets of the blocks (elements)
+  std::vector<int> fo;      // [nb + 1] forward segment offsets (elements); fo[nb] = start of the backward ones
+  std::vector<int> bo;      // [nb + 1] backward segment offsets (bo[0] unused)
+  int segmax = 0;           // largest segment (elements)
   std::vector<int> co;      // [nb + 1] offsets of the blocks' constraint lists in cr
   std::vector<int> cr;      // per block, ascending: rows of A with >= 2 entries touching it
   long long fsize = 0;      // factor elements
@@ -254,17 +268,28 @@ inline int kkt_plan_build(int n, int m, const int* Pp, const int* Pi, const int*
   for (int v = 0; v < n; v++)
     for (int e = pp[v]; e < pp[v + 1]; e++)
       if (std::abs(blk[v] - blk[pc[e]]) > 1) return 2;
-  // factor offsets
+  // factor offsets: the forward segments, then the backward ones
   pl.fo.assign(pl.nb + 1, 0);
-  long long off = 0;
+  pl.bo.assign(pl.nb + 1, 0);
+  long long off = 0, smax = 0;
   for (int k = 0; k < pl.nb; k++) {
     const long long b = pl.bs[k + 1] - pl.bs[k], bp = k ? pl.bs[k] - pl.bs[k - 1] : 0;
     pl.fo[k] = (int)off;
-    off += b * b + 2 * b * bp;
+    const long long seg = kkt_pad4(b * bp) + kkt_pad4(b * b);
+    smax = std::max(smax, seg);
+    off += seg;
     if (off > INT32_MAX) return 1;
   }
   pl.fo[pl.nb] = (int)off;
+  for (int k = 1; k < pl.nb; k++) {
+    const long long b = pl.bs[k + 1] - pl.bs[k], bp = pl.bs[k] - pl.bs[k - 1];
+    pl.bo[k] = (int)off;
+    off += kkt_pad4(b * bp);
+    if (off > INT32_MAX) return 1;
+  }
+  pl.bo[0] = (int)off;
   pl.fsize = off;
+  pl.segmax = (int)smax;
   // constraint rows (two or more entries) touching each block, ascending
   pl.co.assign(pl.nb + 1, 0);
   std::vector<int> rmark(m, -1);

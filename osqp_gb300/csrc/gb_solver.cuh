@@ -115,6 +115,7 @@ struct DevProblem {
   // on-chip workspace for it (set by the kernel)
   KktView<T> kkt;
   T* kws = nullptr;
+  KktPipe* kpipe = nullptr;   // bulk-copy pipeline state of the CTA (static shared memory)
 };
 
 // ---------------------------------------------------------------------------
@@ -605,8 +606,12 @@ struct Solver {
 
     if (direct) {
       // x~ = K^-1 rhs (gb_direct.cuh), written to xp
-      if constexpr (std::is_same<G, BlockGroup>::value)
-        kkt_solve<T>(pr.kkt, kc, kc + n, [&](int i, T v) { xp[i] = v; });
+      if constexpr (std::is_same<G, BlockGroup>::value) {
+        if (pr.kkt.ring >= 2 && pr.kpipe)
+          kkt_solve_pipe<T>(pr.kkt, pr.kpipe, kc, kc + n, kc + kkt_pad4(2LL * n), [&](int i, T v) { xp[i] = v; });
+        else
+          kkt_solve<T>(pr.kkt, kc, kc + n, [&](int i, T v) { xp[i] = v; });
+      }
     } else {
       const int pcg_it = pcg_core(g, eps, sig, rho_s);
       if (pcg_it < 0) return false;
