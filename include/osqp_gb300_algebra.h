@@ -160,6 +160,18 @@ OSQPInt osqp_algebra_init_linsys_solver(LinSysSolver** s, const OSQPMatrix* P, c
  * kernel clears what must start at zero): calls that overlap on the GPU
  * (other threads, other processes' streams of the same library) race and
  * must be serialised by the caller. */
+/* Row structure derived from a matrix's CSC arrays (host copies; no
+ * reference counterpart -- the reference keeps the same arrays inside its
+ * csr_t, algebra/cuda/include/csr_type.h:27-40, built by csr_triu_to_full /
+ * csr_transpose, algebra/cuda/src/cuda_csr.cu:489-628): CSR rowptr (rows + 1),
+ * col and src (nnz each; value k of the rows is CSC value src[k], or -1 for a
+ * structural diagonal added to a symmetric matrix) and, for upper-triangular
+ * storage, diag (n: position of (j, j) in the rows).  The rows are those of
+ * the represented matrix: full symmetric with an explicit diagonal for
+ * is_triu, else of A itself.  Any pointer may be NULL.  Returns the number of
+ * row entries, or -1. */
+OSQPInt osqp_gb300_matrix_rows(const OSQPMatrix* M, OSQPInt* rowptr, OSQPInt* col, OSQPInt* src, OSQPInt* diag);
+
 OSQPInt osqp_gb300_linsys_solve_noalloc(const OSQPMatrix* P, const OSQPMatrix* A, const OSQPVectorf* rho_vec,
                                         const OSQPSettings* settings, OSQPVectorf* b);
 

@@ -30,6 +30,18 @@ OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter, long long
  * counts for the solve in progress only.  Returns 0 on success. */
 OSQPInt osqp_gb300_interrupt(OSQPSolver* solver);
 
+/* Row structure the set-up derived from the caller's CSC arrays (host
+ * copies, for inspection; no reference counterpart -- the reference builds
+ * the same arrays with csr_triu_to_full / csr_transpose,
+ * algebra/cuda/src/cuda_csr.cu:489-628): which = 0 the full symmetric P with an
+ * explicit diagonal (n rows), 1 the rows of A (m rows).  rowptr (rows + 1),
+ * col and src (entries: row entry e holds input value src[e] of the upper
+ * triangle of P / of A, or -1 for a structural diagonal), diag (which = 0: n
+ * positions of the diagonal entries).  Any pointer may be NULL.  Returns the
+ * number of entries, or -1. */
+OSQPInt osqp_gb300_structure(OSQPSolver* solver, OSQPInt which, OSQPInt* rowptr, OSQPInt* col, OSQPInt* src,
+                             OSQPInt* diag);
+
 /* ---- Block-Jacobi preconditioner -------------------------------------------
  * settings->cg_precond = OSQP_GB300_BLOCK_DIAGONAL_PRECONDITIONER (an
  * extension of osqp_precond_type, include/public/osqp_api_constants.h:66-69,
@@ -127,6 +139,11 @@ OSQPInt osqp_gb300_batch_qp_seconds(OSQPBatch* batch, double* seconds);
 
 /* PCG iterations of every QP in the last batch solve (count entries, host memory). */
 OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* batch, long long* pcg_iter);
+
+/* The row structure of QP k of a batch, as osqp_gb300_structure describes
+ * (positions relative to the QP's own arrays). */
+OSQPInt osqp_gb300_batch_structure(OSQPBatch* batch, OSQPInt k, OSQPInt which, OSQPInt* rowptr, OSQPInt* col,
+                                   OSQPInt* src, OSQPInt* diag);
 
 /* rho updates of every QP in the last batch solve (count entries, host memory;
  * OSQPInfo.rho_updates, include/public/osqp_api_types.h:165). */

@@ -559,6 +559,16 @@ OSQPInt* OSQPMatrix_get_i(const OSQPMatrix* M) { return M->i; }
 OSQPInt* OSQPMatrix_get_p(const OSQPMatrix* M) { return M->p; }
 OSQPInt OSQPMatrix_get_nz(const OSQPMatrix* M) { return M->nnz; }
 
+OSQPInt osqp_gb300_matrix_rows(const OSQPMatrix* M, OSQPInt* rowptr, OSQPInt* col, OSQPInt* src, OSQPInt* diag) {
+  if (!M) return -1;
+  const int rows = M->S.rows, nz = M->nnzS;
+  if (rowptr && cudaMemcpy(rowptr, M->S.rowptr, sizeof(int) * (rows + 1), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (col && nz && cudaMemcpy(col, M->S.col, sizeof(int) * nz, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (src && nz && cudaMemcpy(src, M->src, sizeof(int) * nz, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (diag && M->triu && M->n && cudaMemcpy(diag, M->diag, sizeof(int) * M->n, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  return nz;
+}
+
 void OSQPMatrix_update_values(OSQPMatrix* M, const OSQPFloat* Mx_new, const OSQPInt* Mx_new_idx, OSQPInt M_new_n) {
   if (M_new_n <= 0 || !Mx_new) return;
   cudaStream_t s = stream();

@@ -1315,6 +1315,32 @@ extern "C" OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* b, long long* pcg) {
   return 0;
 }
 
+extern "C" OSQPInt osqp_gb300_batch_structure(OSQPBatch* b, OSQPInt k, OSQPInt which, OSQPInt* rowptr, OSQPInt* col,
+                                              OSQPInt* src, OSQPInt* diag) {
+  if (!b || k < 0 || k >= b->count || which < 0 || which > 1) return -1;
+  if (cudaSetDevice(b->device) != cudaSuccess || cudaStreamSynchronize(b->stream) != cudaSuccess) return -1;
+  const BatchInst& I = b->inst[k];
+  const int rows = which == 0 ? I.n : I.m;
+  std::vector<int> rp(rows + 1);
+  const int* grp = which == 0 ? b->B.Prow + I.n_off : b->B.Arow + I.m_off;
+  BT_TRY(cudaMemcpy(rp.data(), grp, sizeof(int) * (rows + 1), cudaMemcpyDeviceToHost));
+  const int base = rp[0], nz = rp[rows] - rp[0];
+  if (rowptr) for (int r = 0; r <= rows; r++) rowptr[r] = rp[r] - base;
+  const int* gcol = which == 0 ? b->B.Pcol : b->B.Acol;
+  const int* gsrc = which == 0 ? b->B.Psrc : b->B.Asrc;
+  if (col && nz) BT_TRY(cudaMemcpy(col, gcol + base, sizeof(int) * nz, cudaMemcpyDeviceToHost));
+  if (src && nz) {
+    BT_TRY(cudaMemcpy(src, gsrc + base, sizeof(int) * nz, cudaMemcpyDeviceToHost));
+    const int off = which == 0 ? I.pt_off : I.a_off;   // positions within the QP's own input arrays
+    for (int e = 0; e < nz; e++) if (src[e] >= 0) src[e] -= off;
+  }
+  if (diag && which == 0) {
+    BT_TRY(cudaMemcpy(diag, b->B.Pdiag + I.n_off, sizeof(int) * I.n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < I.n; i++) diag[i] -= base;
+  }
+  return nz;
+}
+
 extern "C" OSQPInt osqp_gb300_batch_rho_updates(OSQPBatch* b, OSQPInt* rho_updates) {
   if (!b || !rho_updates) return OSQP_WORKSPACE_NOT_INIT_ERROR;
   std::vector<BatchInfo> info(b->count);

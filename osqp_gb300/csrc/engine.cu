@@ -1273,6 +1273,21 @@ extern "C" OSQPInt osqp_gb300_solve_stats(OSQPSolver* solver, OSQPInt* admm_iter
   return 0;
 }
 
+extern "C" OSQPInt osqp_gb300_structure(OSQPSolver* solver, OSQPInt which, OSQPInt* rowptr, OSQPInt* col,
+                                        OSQPInt* src, OSQPInt* diag) {
+  if (!solver || !solver->work || which < 0 || which > 1) return -1;
+  OSQPWorkspace* w = solver->work;
+  if (cudaSetDevice(w->device) != cudaSuccess || cudaStreamSynchronize(w->stream) != cudaSuccess) return -1;
+  const CSR<T>& M = which == 0 ? w->pr.P : w->pr.A;
+  const int rows = which == 0 ? w->n : w->m, nz = which == 0 ? w->nnzPf : w->nnzA;
+  const int* sp = which == 0 ? w->pr.Psrc : w->pr.Asrc;
+  if (rowptr && cudaMemcpy(rowptr, M.rowptr, sizeof(int) * (rows + 1), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (col && nz && cudaMemcpy(col, M.col, sizeof(int) * nz, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (src && nz && cudaMemcpy(src, sp, sizeof(int) * nz, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (diag && which == 0 && cudaMemcpy(diag, w->pr.Pdiag, sizeof(int) * w->n, cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  return nz;
+}
+
 extern "C" OSQPInt osqp_gb300_precond_blocks(OSQPSolver* solver, OSQPFloat* out) {
   if (!solver || !solver->work) return 0;
   OSQPWorkspace* w = solver->work;
