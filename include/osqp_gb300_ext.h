@@ -145,6 +145,13 @@ OSQPInt osqp_gb300_batch_pcg_iters(OSQPBatch* batch, long long* pcg_iter);
 OSQPInt osqp_gb300_batch_structure(OSQPBatch* batch, OSQPInt k, OSQPInt which, OSQPInt* rowptr, OSQPInt* col,
                                    OSQPInt* src, OSQPInt* diag);
 
+/* SM clock cycles of the last batch solve summed over its QPs, per phase of
+ * the ADMM iteration: right-hand side, linear solve, x / z / y updates,
+ * residuals and termination, refactorisation (cycles[0..4]; zeros unless the
+ * batch was set up with OSQP_GB300_PROFILE=1 in the environment).  No
+ * reference counterpart (the reference's profiler_level times host phases). */
+OSQPInt osqp_gb300_batch_phase_cycles(OSQPBatch* batch, double* cycles);
+
 /* rho updates of every QP in the last batch solve (count entries, host memory;
  * OSQPInfo.rho_updates, include/public/osqp_api_types.h:165). */
 OSQPInt osqp_gb300_batch_rho_updates(OSQPBatch* batch, OSQPInt* rho_updates);

@@ -359,6 +359,8 @@ class Batch:
         L.osqp_gb300_batch_rho_updates.restype = I
         L.osqp_gb300_batch_factor_elems.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
         L.osqp_gb300_batch_factor_elems.restype = I
+        L.osqp_gb300_batch_phase_cycles.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.osqp_gb300_batch_phase_cycles.restype = I
 
     @staticmethod
     def pack(problems, float_dtype):
@@ -461,6 +463,12 @@ class Batch:
         out = np.zeros(self.count, np.int32)
         self.L.lib.osqp_gb300_batch_rho_updates(self._h, out.ctypes.data_as(C.POINTER(self.L.I)))
         return out
+
+    def phase_cycles(self):
+        """SM cycles of the last solve per ADMM phase, summed over QPs (needs OSQP_GB300_PROFILE=1 at set-up)."""
+        out = np.zeros(5, np.float64)
+        self.L.lib.osqp_gb300_batch_phase_cycles(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return dict(zip(["rhs", "linsys", "updates", "termination", "refactor"], out.tolist()))
 
     def factor_elems(self):
         """Elements of each QP's direct-solver factor (0 with the indirect solver)."""

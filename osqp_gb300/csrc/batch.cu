@@ -548,6 +548,11 @@ __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out,
     long long a = 0, p = 0;
     for (int k = 0; k < count; k++) { a += st[k].iter; p += st[k].pcg_iters_total; }
     totals[0] = a; totals[1] = p;
+    for (int q = 0; q < 5; q++) {
+      unsigned long long c = 0;
+      for (int k = 0; k < count; k++) c += st[k].prof[q];
+      totals[2 + q] = (long long)c;
+    }
   }
 }
 
@@ -695,6 +700,7 @@ static DevSettings batch_dev_settings(const OSQPSettings* st) {
   d.scaled_termination = st->scaled_termination; d.check_dualgap = st->check_dualgap;
   d.warm_starting = st->warm_starting;
   d.cancel_gen = 0;
+  d.profile = env_int("OSQP_GB300_PROFILE", 0) != 0;
   return d;
 }
 
@@ -939,7 +945,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   size_t o_ctype = pl.take(sizeof(int) * msum), o_st = pl.take(sizeof(SolverScalars) * count);
   size_t o_inst = pl.take(sizeof(BatchInst) * count), o_order = pl.take(sizeof(int) * count);
   size_t o_order2 = pl.take(sizeof(int) * count);
-  size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 2);
+  size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 8);
   size_t o_sq = pl.take(sizeof(T) * nsum), o_sl = pl.take(sizeof(T) * msum), o_su = pl.take(sizeof(T) * msum);
   size_t o_binv = pl.take(sizeof(T) * b->binv_elems);
   size_t o_kperm = pl.take(sizeof(int) * (b->direct ? nsum : 0)), o_kiperm = pl.take(sizeof(int) * (b->direct ? nsum : 0));
@@ -1339,6 +1345,14 @@ extern "C" OSQPInt osqp_gb300_batch_structure(OSQPBatch* b, OSQPInt k, OSQPInt w
     for (int i = 0; i < I.n; i++) diag[i] -= base;
   }
   return nz;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_phase_cycles(OSQPBatch* b, double* cycles) {
+  if (!b || !cycles) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  long long tot[8];
+  BT_TRY(cudaMemcpy(tot, b->d_totals, sizeof(tot), cudaMemcpyDeviceToHost));
+  for (int q = 0; q < 5; q++) cycles[q] = (double)tot[2 + q];
+  return 0;
 }
 
 extern "C" OSQPInt osqp_gb300_batch_rho_updates(OSQPBatch* b, OSQPInt* rho_updates) {

@@ -401,6 +401,7 @@ static DevSettings make_dev_settings(const OSQPSettings* st) {
   d.scaled_termination = st->scaled_termination; d.check_dualgap = st->check_dualgap;
   d.warm_starting = st->warm_starting;
   d.cancel_gen = 0;
+  d.profile = 0;
   return d;
 }
 

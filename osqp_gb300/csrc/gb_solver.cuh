@@ -54,6 +54,7 @@ struct DevSettings {
   // interrupt generation of this solve (> 0): the solve stops when its
   // cancel word holds this value; 0: no interrupts
   int cancel_gen;
+  int profile;   // accumulate per-phase clock cycles of each solve (SolverScalars::prof)
 };
 
 // Per-problem scalar state.  Lives in global memory between launches; during
@@ -81,6 +82,10 @@ struct SolverScalars {
   int cancel;
   int p_parity;
   int kkt_fail;   // direct solver: the last factorisation met a non-positive pivot
+  // DevSettings::profile: SM clock cycles of the last solve, thread 0's view,
+  // per phase: 0 right-hand side, 1 linear solve, 2 x / z / y updates,
+  // 3 residuals and termination, 4 refactorisation / preconditioner refresh
+  unsigned long long prof[5];
 };
 
 template <typename T>
@@ -546,6 +551,8 @@ struct Solver {
     T* __restrict__ xp = pr.xp;
     const bool direct = pr.kkt.nb > 0;
     T* const kc = pr.kws;            // direct: permuted right-hand side
+    const bool prof = s.profile && threadIdx.x == 0;
+    long long pt = prof ? clock64() : 0;
     const int* const kip = pr.kkt.iperm;
 
     // Phase R: rhs = (sigma x - q) + A'(rho .* (z - rho^-1 y)) and, for the
@@ -581,6 +588,7 @@ struct Solver {
     const double rhs_norm = rm0[0];
     const double elapsed = rm0[1];
     const int cancel = rm0[2] > 0.0;
+    if (prof) { const long long t = clock64(); sc->prof[0] += (unsigned long long)(t - pt); pt = t; }
 
     // PCG tolerance (cuda_pcg_interface.cu:32-64), computed once per CTA
     if (threadIdx.x == 0 && !direct) {
@@ -620,6 +628,7 @@ struct Solver {
       sc->elapsed = elapsed;
       sc->cancel = cancel;
     }
+    if (prof) { const long long t = clock64(); sc->prof[1] += (unsigned long long)(t - pt); pt = t; }
 
     // Phase U: x~ = xp, z~ = A xp, then the x / z / y updates (auxil.c:172-229)
     const T al = (T)s.alpha, oma = (T)(1.0 - s.alpha);
@@ -644,7 +653,9 @@ struct Solver {
       });
     }
     __syncthreads();
-    return g.sync();
+    const bool ok = g.sync();
+    if (prof) sc->prof[2] += (unsigned long long)(clock64() - pt);
+    return ok;
   }
 
 
@@ -1201,6 +1212,7 @@ struct Solver {
         sc->t_start = global_ns();
         sc->status = ST_UNSOLVED;
         sc->pcg_iters_total = 0;
+        for (int q = 0; q < 5; q++) sc->prof[q] = 0;
       }
     }
     if (it_lo <= 1 && !s.warm_starting) { cold_start(g); }
@@ -1233,6 +1245,7 @@ struct Solver {
       if (s_flags[0]) { stopped = true; break; }
       can_check = s_flags[1];
       int can_adapt = s_flags[2];
+      const long long t_info = (s.profile && threadIdx.x == 0) ? clock64() : 0;
       if (can_check || can_adapt || iter == 1) { if (!update_info(g, iter)) return false; }
       if (threadIdx.x == 0) {
         s_flags[3] = 0;
@@ -1255,7 +1268,9 @@ struct Solver {
         }
       }
       __syncthreads();
+      if (s.profile && threadIdx.x == 0) sc->prof[3] += (unsigned long long)(clock64() - t_info);
       if (s_flags[3]) { stopped = true; break; }
+      const long long t_fac = (s.profile && threadIdx.x == 0) ? clock64() : 0;
       if (sc->rho_updated) {
         if (s.rho_is_vec) { refresh_rho_vec(g); if (!g.sync()) return false; }
         update_precond(g);
@@ -1267,6 +1282,7 @@ struct Solver {
           break;
         }
       }
+      if (s.profile && threadIdx.x == 0) sc->prof[4] += (unsigned long long)(clock64() - t_fac);
     }
     if (!stopped && it_end < s.max_iter) {
       // suspended at it_hi: no post-loop, no solution store
