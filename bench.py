@@ -66,12 +66,14 @@ def _nx_of(A):
     return int(np.argmax(rowlen != 1))
 
 
-def make_workload(count, steps, seed=3):
-    probs = pb.mpc_batch(count, seed=seed)
+def make_workload(count, steps, seed=3, share=0):
+    """QPs share*count .. (share+1)*count - 1 of the seeded MPC set (a rank's
+    contiguous share under --gpus N) and their bounds for `steps` steps."""
+    probs = pb.mpc_batch(count, seed=seed, start=share * count)
     nxs = [_nx_of(p[2]) for p in probs]
     ls, us = [], []
     for s in range(steps):
-        rg = np.random.default_rng([seed, 7919, s])
+        rg = np.random.default_rng([seed, 7919, s, share])
         lrow, urow = [], []
         for (P, q, A, l, u), nx in zip(probs, nxs):
             l2, u2 = pb.mpc_x0_bounds(l, u, rg.uniform(-1.0, 1.0, nx))
@@ -330,8 +332,10 @@ def gpu_arm(args, probs, ls, us):
     torch.cuda.synchronize(); barrier()
     e2e_s = time.perf_counter() - t0
 
-    # ---- max over ranks ----
+    # ---- max over ranks; per-QP statuses of every rank's share, in order ----
     vals = max_over_ranks([dev_total_ms, e2e_s], dist)
+    from osqp_gb300.router import gather_in_order
+    status_last = gather_in_order({"status": status_last}, dist)["status"]
     if dist is not None:
         dist.destroy_process_group()
     dev_total_ms, e2e_s = float(vals[0]), float(vals[1])
@@ -614,7 +618,8 @@ def main():
               "linsys_solver": args.linsys,
               "preconditioner": ("block-Jacobi 32x32" if args.precond == "block" else "diagonal (Jacobi)") if args.linsys == "indirect" else None,
               "l2": "inputs (~3 GB of CSR data and factors) exceed the 129 MB L2",
-              "parallelism": f"replicas x{world}"}
+              "parallelism": f"data-parallel x{world}: each GPU owns a contiguous share of {args.count} QPs "
+                             "(weak scaling), results gathered in order"}
     metric = "QP solves/s (batched MPC, eps 1e-3)"
 
     if args.impl == "reference":
@@ -633,7 +638,9 @@ def main():
         print(json.dumps(line))
         return
 
-    probs, ls, us = make_workload(args.count, K + W)
+    # each rank owns a contiguous share of count QPs of the whole set (weak
+    # scaling: the set grows with the ranks; no data-path collective)
+    probs, ls, us = make_workload(args.count, K + W, share=rank)
     g = gpu_arm(args, probs, ls, us)
     if rank != 0:
         return

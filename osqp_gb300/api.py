@@ -466,9 +466,10 @@ class Batch:
 
     def phase_cycles(self):
         """SM cycles of the last solve per ADMM phase, summed over QPs (needs OSQP_GB300_PROFILE=1 at set-up)."""
-        out = np.zeros(5, np.float64)
+        out = np.zeros(7, np.float64)
         self.L.lib.osqp_gb300_batch_phase_cycles(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
-        return dict(zip(["rhs", "linsys", "updates", "termination", "refactor"], out.tolist()))
+        return dict(zip(["rhs", "linsys", "updates", "termination", "refactor", "linsys_wait", "linsys_barrier"],
+                        out.tolist()))
 
     def factor_elems(self):
         """Elements of each QP's direct-solver factor (0 with the indirect solver)."""

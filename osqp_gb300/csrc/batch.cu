@@ -313,7 +313,7 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
     pv.kws = (TT*)dsm;
     pv.kpipe = kpipe;
     if (!kpipe) pv.kkt.ring = 0;
-    kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.kkt.bmax, pv.kkt.segmax, pv.kkt.ring) * sizeof(TT)));
+    kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.m, pv.kkt.bmax, pv.kkt.segmax, pv.kkt.ring) * sizeof(TT)));
     __syncthreads();
   }
   if (mode == kModeSolve && dsm_bytes > 0 && !direct) {
@@ -548,7 +548,7 @@ __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out,
     long long a = 0, p = 0;
     for (int k = 0; k < count; k++) { a += st[k].iter; p += st[k].pcg_iters_total; }
     totals[0] = a; totals[1] = p;
-    for (int q = 0; q < 5; q++) {
+    for (int q = 0; q < 7; q++) {
       unsigned long long c = 0;
       for (int k = 0; k < count; k++) c += st[k].prof[q];
       totals[2 + q] = (long long)c;
@@ -894,9 +894,9 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
           if (!prc[k]) {
             // ring slots of the solve's bulk-copy pipeline: as many as fit (at least 2), else none
             int R = kKktRingMax;
-            while (R >= 2 && kkt_ws_bytes(I.n, plans[k].bmax, plans[k].nb, plans[k].segmax, R, (int)sizeof(T)) > b->dsm) R--;
+            while (R >= 2 && kkt_ws_bytes(I.n, I.m, plans[k].bmax, plans[k].nb, plans[k].segmax, R, (int)sizeof(T)) > b->dsm) R--;
             if (R < 2) R = 0;
-            if (kkt_ws_bytes(I.n, plans[k].bmax, plans[k].nb, plans[k].segmax, R, (int)sizeof(T)) > b->dsm) prc[k] = 3;
+            if (kkt_ws_bytes(I.n, I.m, plans[k].bmax, plans[k].nb, plans[k].segmax, R, (int)sizeof(T)) > b->dsm) prc[k] = 3;
             ring[k] = R;
           }
         }
@@ -945,7 +945,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   size_t o_ctype = pl.take(sizeof(int) * msum), o_st = pl.take(sizeof(SolverScalars) * count);
   size_t o_inst = pl.take(sizeof(BatchInst) * count), o_order = pl.take(sizeof(int) * count);
   size_t o_order2 = pl.take(sizeof(int) * count);
-  size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 8);
+  size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 10);
   size_t o_sq = pl.take(sizeof(T) * nsum), o_sl = pl.take(sizeof(T) * msum), o_su = pl.take(sizeof(T) * msum);
   size_t o_binv = pl.take(sizeof(T) * b->binv_elems);
   size_t o_kperm = pl.take(sizeof(int) * (b->direct ? nsum : 0)), o_kiperm = pl.take(sizeof(int) * (b->direct ? nsum : 0));
@@ -1349,9 +1349,9 @@ extern "C" OSQPInt osqp_gb300_batch_structure(OSQPBatch* b, OSQPInt k, OSQPInt w
 
 extern "C" OSQPInt osqp_gb300_batch_phase_cycles(OSQPBatch* b, double* cycles) {
   if (!b || !cycles) return OSQP_WORKSPACE_NOT_INIT_ERROR;
-  long long tot[8];
+  long long tot[10];
   BT_TRY(cudaMemcpy(tot, b->d_totals, sizeof(tot), cudaMemcpyDeviceToHost));
-  for (int q = 0; q < 5; q++) cycles[q] = (double)tot[2 + q];
+  for (int q = 0; q < 7; q++) cycles[q] = (double)tot[2 + q];
   return 0;
 }
 

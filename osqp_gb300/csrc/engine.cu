@@ -70,7 +70,7 @@ __device__ __forceinline__ void attach_direct_ws(DevProblem<TT>& pr, KktPipe* kp
     pr.kws = (TT*)g_engine_dsm;
     pr.kpipe = kpipe;
     if (!kpipe) pr.kkt.ring = 0;
-    kkt_plan_on_chip(pr.kkt, (int*)(g_engine_dsm + kkt_ws_elems(pr.n, pr.kkt.bmax, pr.kkt.segmax, pr.kkt.ring) * sizeof(TT)));
+    kkt_plan_on_chip(pr.kkt, (int*)(g_engine_dsm + kkt_ws_elems(pr.n, pr.m, pr.kkt.bmax, pr.kkt.segmax, pr.kkt.ring) * sizeof(TT)));
     __syncthreads();
   }
 }
@@ -706,9 +706,9 @@ extern "C" OSQPInt osqp_setup(OSQPSolver** solverp, const OSQPCscMatrix* P, cons
     const int blim = kkt_bmax_limit(kBlockThreads, room, (int)sizeof(T));
     const int prc = kkt_plan_build(n, m, Pp.data(), Pi.data(), Ap.data(), Ai.data(), blim, kplan);
     int R = kKktRingMax;
-    while (!prc && R >= 2 && kkt_ws_bytes(n, kplan.bmax, kplan.nb, kplan.segmax, R, (int)sizeof(T)) > room) R--;
+    while (!prc && R >= 2 && kkt_ws_bytes(n, m, kplan.bmax, kplan.nb, kplan.segmax, R, (int)sizeof(T)) > room) R--;
     if (R < 2) R = 0;
-    const long long need = prc ? 0 : kkt_ws_bytes(n, kplan.bmax, kplan.nb, kplan.segmax, R, (int)sizeof(T));
+    const long long need = prc ? 0 : kkt_ws_bytes(n, m, kplan.bmax, kplan.nb, kplan.segmax, R, (int)sizeof(T));
     kring = R;
     if (prc || need > room) {
       fprintf(stderr, "osqp_gb300: the direct KKT solver does not apply to this problem (n=%d, m=%d): %s\n", n, m,

@@ -323,7 +323,15 @@ __device__ __forceinline__ void kkt_bulk_load(void* dst, const void* src, unsign
 // j = nb + t the backward segment of block nb - 1 - t.  A step may refill the
 // slot of a copy no later step needs; at most kv.ring copies are ahead.
 template <typename T, typename XO>
-__device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T* ring, XO xout) {
+__device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T* ring, XO xout,
+                               unsigned long long* prof = nullptr) {
+  // prof (thread 0 only, optional): cycles spent [0] waiting for segments, [1] in barriers
+  long long tw = 0, tb = 0;
+  auto sync = [&]() {
+    const long long t = clock64();   // every thread takes the same barrier
+    __syncthreads();
+    if (prof) tb += clock64() - t;
+  };
   const int nt = blockDim.x, half = nt >> 1;
   const bool lo = (int)threadIdx.x < half;
   const int nb = kv.nb, R = kv.ring, SM = kv.segmax;
@@ -358,7 +366,10 @@ __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T*
     const unsigned Q = q0 + (unsigned)j;
     long long el;
     if (*(volatile int*)&pp->err) return seg(j, el);
-    if (!kkt_wait(&pp->bar[Q % (unsigned)R], (Q / (unsigned)R) & 1u)) {
+    const long long t = prof ? clock64() : 0;
+    const bool ok = kkt_wait(&pp->bar[Q % (unsigned)R], (Q / (unsigned)R) & 1u);
+    if (prof) tw += clock64() - t;
+    if (!ok) {
       *(volatile int*)&pp->err = 1;
       return seg(j, el);
     }
@@ -378,7 +389,7 @@ __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T*
       const T* Si = prev + kkt_pad4((long long)bp * (sp - spp));
       kkt_block_rows(Si, c + sp, bp, bp, half, nt - half, [&](int r, T a) { d[sp + r] = a; });
     }
-    __syncthreads();
+    sync();
   }
   {
     const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
@@ -386,7 +397,7 @@ __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T*
     issue_upto(nb - 1 + R);
     const T* Si = cur + kkt_pad4((long long)b * bp);
     kkt_block_rows(Si, c + s0, b, b, 0, nt, [&](int r, T a) { d[s0 + r] = a; });
-    __syncthreads();
+    sync();
   }
   for (int t = 0; t + 1 < nb; t++) {
     const int k = nb - 1 - t;
@@ -398,11 +409,12 @@ __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T*
     } else {
       for (int r = threadIdx.x - half; r < b; r += nt - half) xout(kv.perm[s0 + r], d[s0 + r]);
     }
-    __syncthreads();
+    sync();
   }
   for (int r = threadIdx.x; r < kv.bs[1]; r += nt) xout(kv.perm[r], d[r]);
   if (threadIdx.x == 0) pp->q = q0 + (unsigned)total;
-  __syncthreads();
+  sync();
+  if (prof) { prof[0] += (unsigned long long)tw; prof[1] += (unsigned long long)tb; }
 }
 
 // Solve K x = b with the factor: c holds the permuted right-hand side on entry

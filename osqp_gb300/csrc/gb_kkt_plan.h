@@ -63,17 +63,21 @@ GB_KKT_HD inline long long kkt_factor_ws_elems(int bmax) {
   return 5LL * bmax * bmax + (long long)kKktTileRows * 2 * bmax + kKktTileRows;
 }
 // Whole on-chip workspace of a direct solve: the factorisation's, or the
-// solve's (two permuted n-vectors and `ring` slots of segmax elements),
-// whichever is larger.
-GB_KKT_HD inline long long kkt_ws_elems(int n, int bmax, int segmax, int ring) {
-  const long long f = kkt_factor_ws_elems(bmax), v = kkt_pad4(2LL * n) + (long long)ring * segmax;
+// ADMM iteration's, whichever is larger.  The iteration's: two permuted
+// n-vectors of the block solve, `ring` slots of segmax elements, then the
+// vectors the sparse products gather -- x~ (n) and w = rho z - y (m).
+GB_KKT_HD inline long long kkt_iter_ws_elems(int n, int m, int segmax, int ring) {
+  return kkt_pad4(2LL * n) + (long long)ring * segmax + kkt_pad4(n) + kkt_pad4(m);
+}
+GB_KKT_HD inline long long kkt_ws_elems(int n, int m, int bmax, int segmax, int ring) {
+  const long long f = kkt_factor_ws_elems(bmax), v = kkt_iter_ws_elems(n, m, segmax, ring);
   return kkt_pad4(f > v ? f : v);
 }
 // Bytes of the whole workspace: the elements above, then copies of the block
 // starts and the forward / backward segment offsets (3 (nb + 1) ints) that
 // every block step reads.
-GB_KKT_HD inline long long kkt_ws_bytes(int n, int bmax, int nb, int segmax, int ring, int elem) {
-  return kkt_ws_elems(n, bmax, segmax, ring) * elem + 12LL * (nb + 1);
+GB_KKT_HD inline long long kkt_ws_bytes(int n, int m, int bmax, int nb, int segmax, int ring, int elem) {
+  return kkt_ws_elems(n, m, bmax, segmax, ring) * elem + 12LL * (nb + 1);
 }
 
 struct KktPlan {

@@ -84,8 +84,9 @@ struct SolverScalars {
   int kkt_fail;   // direct solver: the last factorisation met a non-positive pivot
   // DevSettings::profile: SM clock cycles of the last solve, thread 0's view,
   // per phase: 0 right-hand side, 1 linear solve, 2 x / z / y updates,
-  // 3 residuals and termination, 4 refactorisation / preconditioner refresh
-  unsigned long long prof[5];
+  // 3 residuals and termination, 4 refactorisation / preconditioner refresh;
+  // of the direct solve: 5 waits for factor segments, 6 block-step barriers
+  unsigned long long prof[7];
 };
 
 template <typename T>
@@ -554,13 +555,23 @@ struct Solver {
     const bool prof = s.profile && threadIdx.x == 0;
     long long pt = prof ? clock64() : 0;
     const int* const kip = pr.kkt.iperm;
+    // direct: on-chip copies of the vectors the sparse products gather,
+    // x~ and w = rho z - y (after the block solve's vectors and ring)
+    T* const kxs = direct ? kc + kkt_pad4(2LL * n) + (long long)pr.kkt.ring * pr.kkt.segmax : nullptr;
+    T* const kw = direct ? kxs + kkt_pad4(n) : nullptr;
 
     // Phase R: rhs = (sigma x - q) + A'(rho .* (z - rho^-1 y)) and, for the
     // PCG, t = rho .* (A xp)
     Acc<T> sm0[1];
     T mx0[3] = {T(0), T(-INFINITY), T(-INFINITY)};
+    if (direct) {
+      // w = rho .* z - y (one rounding) on chip, so the product gathers from shared memory
+      for_m(g, m, [&](int j) { kw[j] = fma(vec ? pr.rho_vec[j] : rho_s, z[j], -y[j]); });
+      __syncthreads();
+    }
     rows_rng(g, span_n(g, n), pr.At,
       [&](int j) {
+        if (direct) return kw[j];
         const T rj = vec ? pr.rho_vec[j] : rho_s;
         const T ij = vec ? pr.rho_inv_vec[j] : rinv_s;
         return rj * (z[j] - ij * y[j]);
@@ -616,9 +627,10 @@ struct Solver {
       // x~ = K^-1 rhs (gb_direct.cuh), written to xp
       if constexpr (std::is_same<G, BlockGroup>::value) {
         if (pr.kkt.ring >= 2 && pr.kpipe)
-          kkt_solve_pipe<T>(pr.kkt, pr.kpipe, kc, kc + n, kc + kkt_pad4(2LL * n), [&](int i, T v) { xp[i] = v; });
+          kkt_solve_pipe<T>(pr.kkt, pr.kpipe, kc, kc + n, kc + kkt_pad4(2LL * n),
+                            [&](int i, T v) { xp[i] = v; kxs[i] = v; }, prof ? sc->prof + 5 : nullptr);
         else
-          kkt_solve<T>(pr.kkt, kc, kc + n, [&](int i, T v) { xp[i] = v; });
+          kkt_solve<T>(pr.kkt, kc, kc + n, [&](int i, T v) { xp[i] = v; kxs[i] = v; });
       }
     } else {
       const int pcg_it = pcg_core(g, eps, sig, rho_s);
@@ -639,7 +651,7 @@ struct Solver {
       pr.dx[i] = xn - xo;
     });
     if (m > 0) {
-      rows_rng(g, span_m(g, m), pr.A, [&](int c) { return xp[c]; }, [&](int j, T zt) {
+      rows_rng(g, span_m(g, m), pr.A, [&](int c) { return direct ? kxs[c] : xp[c]; }, [&](int j, T zt) {
         const T ri = vec ? pr.rho_inv_vec[j] : rinv_s;
         const T rr = vec ? pr.rho_vec[j] : rho_s;
         const T zo = z[j];
@@ -1212,7 +1224,7 @@ struct Solver {
         sc->t_start = global_ns();
         sc->status = ST_UNSOLVED;
         sc->pcg_iters_total = 0;
-        for (int q = 0; q < 5; q++) sc->prof[q] = 0;
+        for (int q = 0; q < 7; q++) sc->prof[q] = 0;
       }
     }
     if (it_lo <= 1 && !s.warm_starting) { cold_start(g); }

@@ -91,9 +91,10 @@ def mpc(seed=3, T=None, nx=None, nu=None):
     return sp.triu(P, format="csc"), q, A, l, u
 
 
-def mpc_batch(count=4096, seed=3):
-    """`count` independent MPC instances; instance i uses seed (seed, i)."""
-    return [mpc(Generator(PCG64([seed, i]))) for i in range(count)]
+def mpc_batch(count=4096, seed=3, start=0):
+    """`count` independent MPC instances; instance i uses seed (seed, i), for
+    i = start .. start + count - 1 (a contiguous share of a larger set)."""
+    return [mpc(Generator(PCG64([seed, i]))) for i in range(start, start + count)]
 
 
 def mpc_x0_bounds(l, u, x0):
