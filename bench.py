@@ -1,25 +1,30 @@
 """Benchmark: QP solves/s of the batched GB300 OSQP engine on batched linear MPC.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--count 4096] [--config mpc_batch|large_sparse|svm]
+                    [--count 4096] [--precision f64|f32] [--config mpc_batch|large_sparse|svm]
 
 Workload (default, "mpc_batch"): 4096 seeded linear-MPC QPs of uneven size
 (horizon T~U{10..50}, nx~U{8..40}, nu~U{4..16}; stacked sparse OSQP form,
-FP32 values, int32 indices).  One step is one receding-horizon round: every
-QP receives a new initial state x0 (new l, u) and is solved from a cold start
-to eps_abs = eps_rel = 1e-3.  The QP structures are set up once, outside the
-timed region, as an MPC controller would.
+int32 indices).  One step is one receding-horizon round: every QP receives a
+new initial state x0 (new l, u) and is solved from a cold start to eps_abs =
+eps_rel = 1e-3 with the direct KKT solver.  The QP structures are set up once,
+outside the timed region, as an MPC controller would.
 
   value   QPs solved per second with the new bounds already in HBM (device
-          time of update + solve, CUDA events on the library's stream)
+          time of update + solve, CUDA events on the library's stream), in
+          --precision: f64 (default) follows the builtin algorithm's
+          trajectory; f32 runs FP32 iterates and factors with double-float
+          reductions (`other_precision` reports the other one, one step)
   e2e     the same through the public C API from pinned host memory: the
           new l, u are copied in and x plus the statuses copied out inside
           the timed region (host wall clock around synchronous calls)
   roofline  algorithmic bytes of the solve kernel (osqp_gb300/roofline.py)
             over its CUDA-event time, against the measured HBM copy peak
   cpu_baseline  the FP64 CPU oracle (OSQP's builtin algebra restated; direct
-            LDL^T KKT solver) on the machine's host cores, process pool, over a
-            bounded sample of the same QPs and steps
+            LDL^T KKT solver) on the machine's host cores, process pool, over
+            every QP of the workload, through the same sequence of steps
+  parity_vs_fp64_oracle  per-QP status, objective and iteration agreement
+            with that oracle on the first timed step
 
 --config large_sparse / svm run the single-QP configurations instead of the
 batch (one JSON line each, not the default line): the n=50k / m=100k sparse QP
@@ -29,7 +34,8 @@ GPU path and the FP64 CPU oracle, objective and residual errors).
 
 --impl reference prints the CPU reference arm (the oracle port on all host
 cores) on the same workload.  With --gpus N > 1 (torchrun) every rank solves
-its own replica of the batch (weak scaling) and rank 0 reports the aggregate.
+its own contiguous share of the QP set (weak scaling) and rank 0 reports the
+aggregate.
 """
 from __future__ import annotations
 
@@ -255,7 +261,9 @@ def gpu_arm(args, probs, ls, us):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    lib = load("f32")
+    prec = args.precision
+    lib = load(prec)
+    npf, tpf, w = (np.float32, torch.float32, 4) if prec == "f32" else (np.float64, torch.float64, 8)
     settings = dict(SETTINGS, device=local)
     b = Batch(lib)
     rc = b.setup(probs, **settings)
@@ -265,11 +273,11 @@ def gpu_arm(args, probs, ls, us):
     K, W = args.steps, args.warmup
     nsteps = K + W
     # bounds of every step resident in HBM (device path) and pinned on the host (e2e path)
-    dev_l = [torch.from_numpy(ls[s].astype(np.float32)).to(f"cuda:{local}") for s in range(nsteps)]
-    dev_u = [torch.from_numpy(us[s].astype(np.float32)).to(f"cuda:{local}") for s in range(nsteps)]
-    pin_l = [torch.from_numpy(ls[s].astype(np.float32)).pin_memory() for s in range(nsteps)]
-    pin_u = [torch.from_numpy(us[s].astype(np.float32)).pin_memory() for s in range(nsteps)]
-    x_out = torch.empty(b.nsum, dtype=torch.float32).pin_memory()
+    dev_l = [torch.from_numpy(ls[s].astype(npf)).to(f"cuda:{local}") for s in range(nsteps)]
+    dev_u = [torch.from_numpy(us[s].astype(npf)).to(f"cuda:{local}") for s in range(nsteps)]
+    pin_l = [torch.from_numpy(ls[s].astype(npf)).pin_memory() for s in range(nsteps)]
+    pin_u = [torch.from_numpy(us[s].astype(npf)).pin_memory() for s in range(nsteps)]
+    x_out = torch.empty(b.nsum, dtype=tpf).pin_memory()
     torch.cuda.synchronize()
 
     dist = replica_group(world)
@@ -308,10 +316,10 @@ def gpu_arm(args, probs, ls, us):
         admm_tot += int(sol["iter"].sum()); pcg_tot += int(pcg.sum())
         for k, (P, q, A, l, u) in enumerate(probs):
             if direct:
-                bytes_alg += direct_solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, 4, int(sol["iter"][k]),
+                bytes_alg += direct_solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, w, int(sol["iter"][k]),
                                                 int(felems[k]), int(rup[k]), SETTINGS["check_termination"])
             else:
-                bytes_alg += solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, 4, int(sol["iter"][k]),
+                bytes_alg += solve_bytes(P.shape[0], A.shape[0], nnz_pf[k], A.nnz, w, int(sol["iter"][k]),
                                          int(pcg[k]), SETTINGS["check_termination"],
                                          SETTINGS.get("cg_precond", 1) == BLOCK_DIAGONAL_PRECONDITIONER)
     torch.cuda.synchronize(); barrier()
@@ -362,17 +370,60 @@ def gpu_arm(args, probs, ls, us):
         value=whole_job_rate(count * K, world, dev_total_ms * 1e-3),
         ms_per_step=dev_total_ms / K,
         e2e_value=whole_job_rate(count * K, world, e2e_s),
-        h2d=2 * 4 * int(b.msum), d2h=4 * int(b.nsum) + 40 * count,
+        h2d=2 * w * int(b.msum), d2h=w * int(b.nsum) + 40 * count,
         solve_ms=float(np.mean(solve_ms)),
         achieved_gbs=bytes_alg / K / (np.mean(solve_ms) * 1e-3) / 1e9,
         bytes_per_launch=bytes_alg / K,
         admm_per_qp=admm_tot / (count * K), pcg_per_qp=pcg_tot / (count * K),
         status_counts={int(k): int(v) for k, v in zip(*np.unique(status_last, return_counts=True))},
         first=first, launches=launches, clocks=clk, plain=plain, rank=rank, world=world, tile=tile,
-        factor_bytes=float(np.sum(felems)) * 4 if direct else None,
+        factor_bytes=float(np.sum(felems)) * w if direct else None,
     )
     b.cleanup()
     return out
+
+
+def precision_leg(prec, probs, ls, us, W):
+    """The batched direct solve in the other precision on the same QPs and
+    step sequence: W untimed steps, then one timed step (device time)."""
+    from osqp_gb300 import load
+    from osqp_gb300.api import Batch
+    b = Batch(load(prec))
+    assert b.setup(probs, **dict(SETTINGS)) == 0
+    for s in range(W):
+        b.update(l=ls[s], u=us[s]); b.solve()
+    b.update(l=ls[W], u=us[W]); b.solve()
+    ms = b.step_ms()
+    st = b.stats()
+    sol = b.solution()
+    b.cleanup()
+    return {"precision": prec, "solves_per_s": len(probs) / (ms * 1e-3), "ms_per_step": ms,
+            "admm_iters_per_qp": st["admm_iter"] / len(probs),
+            "first": {"status": sol["status"].copy(), "obj": sol["obj"].copy(), "iter": sol["iter"].copy()}}
+
+
+def parity(first, cpu, count):
+    """Per-QP status, objective and ADMM iteration agreement with the oracle's
+    results of the same step."""
+    st_g, st_o = first["status"], np.array([cpu["first"][i][0] for i in range(count)])
+    errs, ratio = [], []
+    for i in range(count):
+        if st_o[i] == 1 and st_g[i] == 1:
+            oo = cpu["first"][i][1]
+            errs.append(abs(float(first["obj"][i]) - oo) / max(1.0, abs(oo)))
+            ratio.append(float(first["iter"][i]) / max(1, cpu["first"][i][2]))
+    errs, ratio = np.array(errs), np.array(ratio)
+    return {"qps": count, "status_mismatches": int(np.sum(st_g != st_o)),
+            "objective_rel_err": {"max": float(errs.max()), "p99": float(np.percentile(errs, 99)),
+                                  "median": float(np.median(errs)),
+                                  "fraction_le_1e-4": float(np.mean(errs <= 1e-4))},
+            "admm_iteration_ratio": {"median": float(np.median(ratio)),
+                                     "fraction_equal": float(np.mean(ratio == 1.0)),
+                                     "fraction_within_10pct": float(np.mean(np.abs(ratio - 1) <= 0.1))},
+            "oracle_admm_iters_per_qp": float(np.mean([cpu["first"][i][2] for i in range(count)])),
+            "against": "FP64 oracle, builtin algorithm (direct LDL' KKT solve): same QPs, same sequence of "
+                       "bound updates and solves (its rho state carried from step to step as on the GPU), "
+                       "the first timed step compared"}
 
 
 def indirect_leg(probs, ls, us, W):
@@ -600,6 +651,11 @@ def main():
                          "indirect: the reduced-KKT PCG)")
     ap.add_argument("--indirect-compare", type=int, default=1, help="also time one step of the PCG path")
     ap.add_argument("--cpu-oracle", type=int, default=1, help="FP64 CPU oracle over every QP of one step")
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32"],
+                    help="arithmetic of the measured batched solve (f64: the builtin algorithm's trajectory; "
+                         "f32: FP32 iterates and factor with double-float reductions)")
+    ap.add_argument("--other-precision", type=int, default=1,
+                    help="also time one step in the other precision, with its parity")
     args = ap.parse_args()
     SETTINGS["max_iter"] = args.max_iter
     SETTINGS["linsys_solver"] = 1 if args.linsys == "direct" else 2
@@ -615,7 +671,7 @@ def main():
                           "new x0 per step, cold solve to eps 1e-3",
               "qps_per_step": args.count, "eps": 1e-3, "settings": "rho_is_vec=1, check_termination=5, "
               "adaptive_rho, scaling=10, check_dualgap=1",
-              "linsys_solver": args.linsys,
+              "linsys_solver": args.linsys, "precision": args.precision,
               "preconditioner": ("block-Jacobi 32x32" if args.precond == "block" else "diagonal (Jacobi)") if args.linsys == "indirect" else None,
               "l2": "inputs (~3 GB of CSR data and factors) exceed the 129 MB L2",
               "parallelism": f"data-parallel x{world}: each GPU owns a contiguous share of {args.count} QPs "
@@ -646,36 +702,24 @@ def main():
         return
     direct = SETTINGS["linsys_solver"] == 1
     indirect = indirect_leg(probs, ls, us, W) if (direct and args.indirect_compare) else None
+    other = "f32" if args.precision == "f64" else "f64"
+    leg2 = precision_leg(other, probs, ls, us, W) if (direct and args.other_precision) else None
     served = serve_leg(args) if args.serve_rate > 0 else None
     peak, peak_kind = measured_peak()
     sizes_m = [p[2].shape[0] for p in probs]
-    # the FP64 oracle on the host cores: every QP of the first timed step
-    cpu = cpu_arm(probs, [ls[W]], [us[W]], sizes_m, steps_timed=1) if args.cpu_oracle else None
-    parity = None
-    if cpu:
-        f = g["first"]
-        st_g, st_o = f["status"], np.array([cpu["first"][i][0] for i in range(len(probs))])
-        errs, ratio = [], []
-        for i in range(len(probs)):
-            if st_o[i] == 1 and st_g[i] == 1:
-                oo = cpu["first"][i][1]
-                errs.append(abs(float(f["obj"][i]) - oo) / max(1.0, abs(oo)))
-                ratio.append(float(f["iter"][i]) / max(1, cpu["first"][i][2]))
-        errs, ratio = np.array(errs), np.array(ratio)
-        parity = {"qps": len(probs), "status_mismatches": int(np.sum(st_g != st_o)),
-                  "objective_rel_err": {"max": float(errs.max()), "p99": float(np.percentile(errs, 99)),
-                                        "median": float(np.median(errs)),
-                                        "fraction_le_1e-4": float(np.mean(errs <= 1e-4))},
-                  "admm_iteration_ratio": {"median": float(np.median(ratio)),
-                                           "fraction_equal": float(np.mean(ratio == 1.0)),
-                                           "fraction_within_10pct": float(np.mean(np.abs(ratio - 1) <= 0.1))},
-                  "oracle_admm_iters_per_qp": float(np.mean([cpu["first"][i][2] for i in range(len(probs))])),
-                  "against": "FP64 oracle, builtin algorithm (direct LDL' KKT solve), same QPs and step"}
+    # the FP64 oracle on the host cores: every QP, through the warm-up steps
+    # and the first timed step (same update / solve sequence as the GPU run)
+    cpu = cpu_arm(probs, ls[:W + 1], us[:W + 1], sizes_m, steps_timed=1, steps_warm=W) if args.cpu_oracle else None
+    par = parity(g["first"], cpu, len(probs)) if cpu else None
+    if leg2 is not None:
+        first2 = leg2.pop("first")
+        leg2["parity_vs_fp64_oracle"] = parity(first2, cpu, len(probs)) if cpu else None
     tr = TRAFFIC_PER_ALGORITHMIC_BYTE[SETTINGS["linsys_solver"]]
     line = dict(
         metric=metric, value=g["value"], unit="solves/s", n_gpus=world, steps=K, warmup=W,
         ms_per_step=g["ms_per_step"], higher_is_better=True, scaling="weak", vs_baseline=None,
-        dtype="f32 (FP64-accurate double-float reductions)", data="synthetic (seeded)", config=config,
+        dtype=("f64" if args.precision == "f64" else "f32 (FP64-accurate double-float reductions)"),
+        data="synthetic (seeded)", config=config,
         e2e={"value": g["e2e_value"], "unit": "solves/s", "h2d_bytes_per_step": g["h2d"],
              "d2h_bytes_per_step": g["d2h"]},
         roofline={"bound": "hbm", "achieved": g["achieved_gbs"], "peak": peak, "unit": "GB/s",
@@ -693,7 +737,8 @@ def main():
         plain_gpu_solves_per_s=g["plain"],
         batched_over_plain=(g["value"] / g["plain"]) if g["plain"] else None,
         admm_iters_per_qp=g["admm_per_qp"], pcg_iters_per_qp=g["pcg_per_qp"],
-        status_counts=g["status_counts"], parity_vs_fp64_oracle=parity,
+        status_counts=g["status_counts"], parity_vs_fp64_oracle=par,
+        other_precision=leg2,
         indirect=indirect,
         spmv_tile_entries_per_lane=g["tile"],
         served=served,

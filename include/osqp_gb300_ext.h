@@ -147,9 +147,14 @@ OSQPInt osqp_gb300_batch_structure(OSQPBatch* batch, OSQPInt k, OSQPInt which, O
 
 /* SM clock cycles of the last batch solve summed over its QPs, per phase of
  * the ADMM iteration: right-hand side, linear solve, x / z / y updates,
- * residuals and termination, refactorisation, and of the direct solve's
- * block steps the waits for factor segments and the barriers (cycles[0..6],
- * thread 0's view; zeros unless the
+ * residuals and termination, refactorisation; of the direct solve's block
+ * steps the waits for factor segments, the barriers, the forward and the
+ * backward sweep; the sparse products of the right-hand side and of the
+ * updates; the issuing of the direct solve's bulk copies (cycles[0..11],
+ * thread 0's view, the last by the issuing thread), then counts of direct
+ * solves: all, through the bulk-copy ring, and of those the ones that read
+ * the factor from global memory after a failed wait (cycles[12..14];
+ * cycles[15] unused); zeros unless the
  * batch was set up with OSQP_GB300_PROFILE=1 in the environment).  No
  * reference counterpart (the reference's profiler_level times host phases). */
 OSQPInt osqp_gb300_batch_phase_cycles(OSQPBatch* batch, double* cycles);

@@ -466,9 +466,11 @@ class Batch:
 
     def phase_cycles(self):
         """SM cycles of the last solve per ADMM phase, summed over QPs (needs OSQP_GB300_PROFILE=1 at set-up)."""
-        out = np.zeros(7, np.float64)
+        out = np.zeros(16, np.float64)
         self.L.lib.osqp_gb300_batch_phase_cycles(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
-        return dict(zip(["rhs", "linsys", "updates", "termination", "refactor", "linsys_wait", "linsys_barrier"],
+        return dict(zip(["rhs", "linsys", "updates", "termination", "refactor", "linsys_wait", "linsys_barrier",
+                         "linsys_forward", "linsys_backward", "rhs_spmv", "updates_spmv", "linsys_issue",
+                         "direct_solves", "direct_solves_ring", "direct_solves_global", "unused"],
                         out.tolist()))
 
     def factor_elems(self):

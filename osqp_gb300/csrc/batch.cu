@@ -313,7 +313,8 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
     pv.kws = (TT*)dsm;
     pv.kpipe = kpipe;
     if (!kpipe) pv.kkt.ring = 0;
-    kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.m, pv.kkt.bmax, pv.kkt.segmax, pv.kkt.ring) * sizeof(TT)));
+    kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.m, pv.kkt.bmax, pv.kkt.segmax, pv.kkt.ring) * sizeof(TT)),
+                     pv.n);
     __syncthreads();
   }
   if (mode == kModeSolve && dsm_bytes > 0 && !direct) {
@@ -548,7 +549,7 @@ __global__ void k_batch_info(const SolverScalars* st, int count, BatchInfo* out,
     long long a = 0, p = 0;
     for (int k = 0; k < count; k++) { a += st[k].iter; p += st[k].pcg_iters_total; }
     totals[0] = a; totals[1] = p;
-    for (int q = 0; q < 7; q++) {
+    for (int q = 0; q < kProfSlots; q++) {
       unsigned long long c = 0;
       for (int k = 0; k < count; k++) c += st[k].prof[q];
       totals[2 + q] = (long long)c;
@@ -904,10 +905,12 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     for (auto& th : pool) th.join();
     for (int k = 0; k < count; k++) {
       if (prc[k]) {
-        fprintf(stderr, "osqp_gb300 batch: direct KKT solve does not apply to QP %d (n=%d, m=%d): %s\n", k,
+        fprintf(stderr, "osqp_gb300 batch: direct KKT solve does not apply to QP %d (n=%d, m=%d): %s "
+                "(at most %d variables per block, %d bytes of shared memory per CTA)\n", k,
                 b->inst[k].n, b->inst[k].m,
                 prc[k] == 1 ? "a block of its block-tridiagonal ordering exceeds the on-chip limit"
-                : prc[k] == 3 ? "its solve vectors exceed the on-chip workspace" : "inconsistent structure");
+                : prc[k] == 3 ? "its solve vectors exceed the on-chip workspace" : "inconsistent structure",
+                blim, b->dsm);
         delete b;
         return OSQP_LINSYS_SOLVER_INIT_ERROR;
       }
@@ -945,7 +948,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   size_t o_ctype = pl.take(sizeof(int) * msum), o_st = pl.take(sizeof(SolverScalars) * count);
   size_t o_inst = pl.take(sizeof(BatchInst) * count), o_order = pl.take(sizeof(int) * count);
   size_t o_order2 = pl.take(sizeof(int) * count);
-  size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * 10);
+  size_t o_misc = pl.take(sizeof(int) * 8), o_info = pl.take(sizeof(BatchInfo) * count), o_tot = pl.take(sizeof(long long) * (2 + kProfSlots));
   size_t o_sq = pl.take(sizeof(T) * nsum), o_sl = pl.take(sizeof(T) * msum), o_su = pl.take(sizeof(T) * msum);
   size_t o_binv = pl.take(sizeof(T) * b->binv_elems);
   size_t o_kperm = pl.take(sizeof(int) * (b->direct ? nsum : 0)), o_kiperm = pl.take(sizeof(int) * (b->direct ? nsum : 0));
@@ -1233,6 +1236,24 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
   if (!rc) cudaMemcpyAsync(snap + off, B.st, sbytes, cudaMemcpyDeviceToDevice, s);
   if (!rc && bbytes) cudaMemcpyAsync(snap + off + sbytes, B.Binv, bbytes, cudaMemcpyDeviceToDevice, s);
   if (!rc) cudaMemcpyAsync(dbuf, sample.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s);
+  // the direct solver refactors when a probe changes rho: keep the sampled
+  // QPs' factors too
+  T* fsnap = nullptr;
+  std::vector<std::pair<long long, long long>> fsl;   // (offset, elements) of each sampled factor
+  if (!rc && b->direct) {
+    long long tot = 0;
+    for (int k : sample) {
+      const long long o = b->inst[k].kf_off, e = (k + 1 < b->count ? b->inst[k + 1].kf_off : b->kf_total) - o;
+      fsl.push_back({o, e});
+      tot += e;
+    }
+    if (cudaMallocAsync((void**)&fsnap, sizeof(T) * (size_t)std::max(1LL, tot), s) != cudaSuccess) rc = OSQP_MEM_ALLOC_ERROR;
+    long long fo = 0;
+    for (size_t i = 0; !rc && i < fsl.size(); i++) {
+      cudaMemcpyAsync(fsnap + fo, B.kF + fsl[i].first, sizeof(T) * fsl[i].second, cudaMemcpyDeviceToDevice, s);
+      fo += fsl[i].second;
+    }
+  }
   LaunchBufs lb{dbuf, ns, dbuf + 2 * (size_t)ns, dbuf + ns};
   float best_ms = 1e30f, default_ms = 1e30f;
   for (int cand : {kDefaultPerLane, 4, 16}) {
@@ -1268,6 +1289,14 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
     cudaMemcpyAsync(B.st, snap + off, sbytes, cudaMemcpyDeviceToDevice, s);
     if (bbytes) cudaMemcpyAsync(B.Binv, snap + off + sbytes, bbytes, cudaMemcpyDeviceToDevice, s);
     cudaFreeAsync(snap, s);
+  }
+  if (fsnap) {
+    long long fo = 0;
+    for (size_t i = 0; i < fsl.size(); i++) {
+      cudaMemcpyAsync(B.kF + fsl[i].first, fsnap + fo, sizeof(T) * fsl[i].second, cudaMemcpyDeviceToDevice, s);
+      fo += fsl[i].second;
+    }
+    cudaFreeAsync(fsnap, s);
   }
   if (dbuf) cudaFreeAsync(dbuf, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) rc = OSQP_ALGEBRA_LOAD_ERROR;
@@ -1349,9 +1378,9 @@ extern "C" OSQPInt osqp_gb300_batch_structure(OSQPBatch* b, OSQPInt k, OSQPInt w
 
 extern "C" OSQPInt osqp_gb300_batch_phase_cycles(OSQPBatch* b, double* cycles) {
   if (!b || !cycles) return OSQP_WORKSPACE_NOT_INIT_ERROR;
-  long long tot[10];
+  long long tot[2 + kProfSlots];
   BT_TRY(cudaMemcpy(tot, b->d_totals, sizeof(tot), cudaMemcpyDeviceToHost));
-  for (int q = 0; q < 7; q++) cycles[q] = (double)tot[2 + q];
+  for (int q = 0; q < kProfSlots; q++) cycles[q] = (double)tot[2 + q];
   return 0;
 }
 

@@ -70,7 +70,8 @@ __device__ __forceinline__ void attach_direct_ws(DevProblem<TT>& pr, KktPipe* kp
     pr.kws = (TT*)g_engine_dsm;
     pr.kpipe = kpipe;
     if (!kpipe) pr.kkt.ring = 0;
-    kkt_plan_on_chip(pr.kkt, (int*)(g_engine_dsm + kkt_ws_elems(pr.n, pr.m, pr.kkt.bmax, pr.kkt.segmax, pr.kkt.ring) * sizeof(TT)));
+    kkt_plan_on_chip(pr.kkt, (int*)(g_engine_dsm + kkt_ws_elems(pr.n, pr.m, pr.kkt.bmax, pr.kkt.segmax, pr.kkt.ring) * sizeof(TT)),
+                     pr.n);
     __syncthreads();
   }
 }

@@ -25,6 +25,7 @@ namespace gb {
 constexpr int kMaxSum = 8;   // FP64 sum slots per reduction
 constexpr int kMaxMax = 24;  // FP64 max slots per reduction
 constexpr int kWarp = 32;
+constexpr int kProfSlots = 16;   // per-phase cycle counters of a solve (DevSettings::profile)
 
 // Spin limit of the grid barrier: ~2^24 polls with 64 ns back-off is roughly
 // one second of waiting before the kernel records an error and returns.

@@ -16,13 +16,19 @@
 // reduced form of the builtin's solve (qdldl_interface.c:431-466 gives the
 // same x~ and z~ in exact arithmetic).
 //
-// The solve streams the factor through shared memory: each block's segment
+// A solve is a chain of dependent block steps, each a few small dense
+// products, so it runs on a small group of warps (two halves of kkt_half(bmax)
+// threads, one thread per block row, column-major blocks so that the threads
+// of a step read consecutive words) synchronised by a named barrier; the other
+// warps of the CTA wait once at the end instead of taking every step's
+// barrier.  The factor streams through shared memory: each block's segment
 // (gb_kkt_plan.h) is one bulk copy (cp.async.bulk, the TMA engine's untiled
-// form) into a ring of `ring` slots, issued by one thread several segments
-// ahead of use and tracked by one mbarrier per slot, so the dependent chain of
-// block steps reads only shared memory.  Waits are bounded: a copy that does
-// not arrive within the limit makes the solve read that segment from global
-// memory instead (and records it in the pipe's error word).
+// form) into a ring of `ring` slots, issued by a producer warp outside the
+// group and tracked by a "full" mbarrier per slot; the group hands a slot back
+// through its "empty" mbarrier when no later step needs it, so issuing never
+// delays the chain.  Waits are bounded: a copy that does not arrive within the
+// limit makes the solve read that segment from global memory instead (and
+// records it in the pipe's error word).
 //
 // Everything is deterministic: each entry has one owner thread and a fixed
 // summation order, so a QP's factor and solutions do not depend on the rest
@@ -35,9 +41,6 @@
 #include "gb_kkt_plan.h"
 
 namespace gb {
-
-// Lanes per row of the dense block products.
-constexpr int kKktLanes = 8;
 
 template <typename T>
 struct KktView {
@@ -169,12 +172,14 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
         S[i * b + j] = v;
         S[j * b + i] = v;
       }
+      // forward segment: G_k column-major (entry (i, j) at j b + i); backward
+      // segment: G_k' column-major, which is G_k row-major
       T* Gg = Fk;
       T* GTg = kv.F + kv.bo[k];
       for (int o = tid; o < b * bp; o += nt) {
-        Gg[o] = G[o];
-        const int j = o / b, i = o - j * b;   // G' is bp x b
-        GTg[o] = G[i * bp + j];
+        const int j = o / b, i = o - j * b;
+        Gg[o] = G[i * bp + j];
+        GTg[o] = G[o];
       }
       __syncthreads();
     }
@@ -215,76 +220,82 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
   return true;
 }
 
-// fn(r, sum_j M[r][j] v[j]) for the rows r < rows of a row-major rows x cols
-// block, by sub-warps of kKktLanes lanes over threads [t0, t0 + tn); fn runs
-// on the sub-warp's first lane.  Loop bounds are uniform over each warp (t0
-// and tn multiples of 32).
-// Entries of a block row a lane loads before it multiplies (cols up to
-// kKktLanes x kKktRowChunk per round): the loads of a round are independent,
-// so a block row costs one memory latency per round, not one per entry.
-constexpr int kKktRowChunk = 8;
+// Threads in each half of the solve group: at least the largest block, a
+// whole number of warps.
+__host__ __device__ inline int kkt_half(int bmax) { return bmax <= 32 ? 32 : ((bmax + 31) & ~31); }
 
-template <typename T, typename FN>
-__device__ __forceinline__ void kkt_block_rows(const T* __restrict__ M, const T* v, int rows, int cols, int t0,
-                                               int tn, FN fn) {
-  const int t = threadIdx.x - t0;
-  const int sub = t / kKktLanes, sl = t % kKktLanes;
-  const int per = tn / kKktLanes;
-  for (int base = 0; base < rows; base += per) {
-    const int r = base + sub;
-    T a = T(0);
-    if (r < rows) {
-      const T* Mr = M + (size_t)r * cols;
-      for (int j0 = sl; j0 < cols; j0 += kKktLanes * kKktRowChunk) {
-        T mv[kKktRowChunk];
-#pragma unroll
-        for (int u = 0; u < kKktRowChunk; u++) {
-          const int j = j0 + u * kKktLanes;
-          mv[u] = j < cols ? Mr[j] : T(0);
-        }
-#pragma unroll
-        for (int u = 0; u < kKktRowChunk; u++) {
-          const int j = j0 + u * kKktLanes;
-          if (j < cols) a += mv[u] * v[j];
-        }
-      }
-    }
-    a = subwarp_sum<kKktLanes>(a);
-    if (r < rows && sl == 0) fn(r, a);
+// sum_j M[j rows + r] v[j]: row r of a column-major rows x cols block, by one
+// thread, in four interleaved partial sums (fixed order).
+template <typename T>
+__device__ __forceinline__ T kkt_col_dot(const T* __restrict__ M, const T* __restrict__ v, int rows, int cols,
+                                         int r) {
+  T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+  int j = 0;
+  for (; j + 4 <= cols; j += 4) {
+    a0 += M[(size_t)j * rows + r] * v[j];
+    a1 += M[(size_t)(j + 1) * rows + r] * v[j + 1];
+    a2 += M[(size_t)(j + 2) * rows + r] * v[j + 2];
+    a3 += M[(size_t)(j + 3) * rows + r] * v[j + 3];
   }
+  for (; j < cols; j++) a0 += M[(size_t)j * rows + r] * v[j];
+  return (a0 + a1) + (a2 + a3);
 }
 
-// Copy the block starts and segment offsets (read at every block step) to
-// on-chip memory `dst` (3 (nb + 1) ints) and point kv at the copies.
+// Barrier of the solve group only (named barrier 1; `threads` a multiple of 32).
+__device__ __forceinline__ void kkt_group_sync(int threads) {
+  asm volatile("bar.sync 1, %0;" :: "r"(threads) : "memory");
+}
+
+// Copy the block starts and segment offsets (read at every block step) and
+// the permutation of the n variables and its inverse (read by every
+// right-hand side and solution) to on-chip memory `dst` (3 (nb + 1) + 2 n
+// ints) and point kv at the copies.
 template <typename T>
-__device__ __forceinline__ void kkt_plan_on_chip(KktView<T>& kv, int* dst) {
+__device__ __forceinline__ void kkt_plan_on_chip(KktView<T>& kv, int* dst, int n) {
   const int w = kv.nb + 1;
   for (int k = threadIdx.x; k < w; k += blockDim.x) { dst[k] = kv.bs[k]; dst[w + k] = kv.fo[k]; dst[2 * w + k] = kv.bo[k]; }
+  int* pm = dst + 3 * w;
+  int* ip = pm + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) { pm[i] = kv.perm[i]; ip[i] = kv.iperm[i]; }
   kv.bs = dst;
   kv.fo = dst + w;
   kv.bo = dst + 2 * w;
+  kv.perm = pm;
+  kv.iperm = ip;
 }
 
 // ---------------------------------------------------------------------------
-// Bulk-copy pipeline state of a CTA: one mbarrier per ring slot and the number
-// of copies issued so far (copy Q goes to slot Q % ring; its wait parity is
-// (Q / ring) & 1).  Lives in static shared memory; kkt_pipe_init once per
-// kernel before the first solve.
+// Bulk-copy pipeline state of a CTA: per ring slot a "full" and an "empty"
+// mbarrier and the number of phases each has completed before the current
+// solve.  Copy j of a solve goes to slot j % ring and is the (fph[s] + j /
+// ring)-th use of that slot, so its parities follow from these counts even
+// when consecutive solves (QPs of different sizes) use different ring sizes.
+// Lives in static shared memory; kkt_pipe_init once per kernel before the
+// first solve.
 // ---------------------------------------------------------------------------
 struct KktPipe {
-  unsigned long long bar[kKktRingMax];
-  unsigned q;
-  int err;
+  unsigned long long bar[kKktRingMax];     // "full": copy landed in the slot
+  unsigned long long empty[kKktRingMax];   // "empty": the group released the slot
+  unsigned fph[kKktRingMax];               // completed phases of bar[s]
+  unsigned eph[kKktRingMax];               // completed phases of empty[s]
+  int err;                                 // a wait failed: read the factor from global memory
+  int issued;                              // copies of the current solve issued so far
+  int fail;                                // first copy of the current solve read from global memory
 };
 
 __device__ __forceinline__ unsigned kkt_smem(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void kkt_pipe_init(KktPipe* pp) {
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kKktRingMax; s++)
+    for (int s = 0; s < kKktRingMax; s++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(kkt_smem(&pp->bar[s])) : "memory");
-    pp->q = 0;
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(kkt_smem(&pp->empty[s])) : "memory");
+      pp->fph[s] = 0;
+      pp->eph[s] = 0;
+    }
     pp->err = 0;
+    pp->issued = 0;
+    pp->fail = 0x7fffffff;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -310,34 +321,38 @@ __device__ __forceinline__ bool kkt_wait(unsigned long long* bar, unsigned parit
 }
 
 // One bulk copy global -> shared of `bytes` (multiple of 16, both addresses
-// 16-byte aligned), completing a transaction on `bar`.  One thread.
+// 16-byte aligned), completing a transaction on `bar`.  One thread; earlier
+// generic-proxy accesses of the slot are ordered before it by the "empty"
+// handshake within a solve and by one fence.proxy.async per solve.
 __device__ __forceinline__ void kkt_bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(kkt_smem(bar)), "r"(bytes) : "memory");
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                :: "r"(kkt_smem(dst)), "l"(src), "r"(bytes), "r"(kkt_smem(bar)) : "memory");
 }
 
+__device__ __forceinline__ void kkt_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(kkt_smem(bar)) : "memory");
+}
+
 // The solve of kkt_solve with the factor streamed through `ring` (kv.ring
 // slots of kv.segmax elements).  Copies j = 0..nb-1 are the forward segments,
-// j = nb + t the backward segment of block nb - 1 - t.  A step may refill the
-// slot of a copy no later step needs; at most kv.ring copies are ahead.
+// j = nb + t the backward segment of block nb - 1 - t; copy j goes to slot
+// j % ring.  The producer (the first thread after the group) issues copy j
+// once the group released copy j - ring; the group releases a copy after the
+// step that last reads it, so every copy of a solve is released by its end.
+// Needs blockDim.x >= 2 kkt_half(bmax) + 32.
 template <typename T, typename XO>
 __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T* ring, XO xout,
-                               unsigned long long* prof = nullptr) {
-  // prof (thread 0 only, optional): cycles spent [0] waiting for segments, [1] in barriers
-  long long tw = 0, tb = 0;
-  auto sync = [&]() {
-    const long long t = clock64();   // every thread takes the same barrier
-    __syncthreads();
-    if (prof) tb += clock64() - t;
-  };
-  const int nt = blockDim.x, half = nt >> 1;
-  const bool lo = (int)threadIdx.x < half;
+                               unsigned long long* prof = nullptr, unsigned long long* prof_issue = nullptr) {
+  // prof (thread 0 only, optional): cycles spent [0] waiting for segments, [1]
+  // in group barriers, [2] in the forward sweep, [3] in the backward sweep
+  const int H = kkt_half(kv.bmax), GT = 2 * H;
+  const int tid = threadIdx.x;
   const int nb = kv.nb, R = kv.ring, SM = kv.segmax;
-  const unsigned q0 = pp->q;
   const int total = 2 * nb - 1;
-  int issued = 0;                                     // thread 0's count
+  // parity of the wait for copy j (full) and of the release of copy j (empty)
+  auto fpar = [&](int j) { return (pp->fph[j % R] + (unsigned)(j / R)) & 1u; };
+  auto epar = [&](int j) { return (pp->eph[j % R] + (unsigned)(j / R)) & 1u; };
   auto seg = [&](int j, long long& elems) -> const T* {
     if (j < nb) {
       const long long b = kv.bs[j + 1] - kv.bs[j], bp = j ? kv.bs[j] - kv.bs[j - 1] : 0;
@@ -349,115 +364,174 @@ __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T*
     elems = kkt_pad4(b * bp);
     return kv.F + kv.bo[k];
   };
-  auto slot = [&](int j) { return ring + (size_t)((q0 + (unsigned)j) % (unsigned)R) * SM; };
-  auto issue_upto = [&](int lim) {
-    if (threadIdx.x == 0) {
-      const int end = lim < total ? lim : total;
-      for (; issued < end; issued++) {
-        long long el;
-        const T* g = seg(issued, el);
-        kkt_bulk_load(slot(issued), g, (unsigned)(el * sizeof(T)), &pp->bar[(q0 + (unsigned)issued) % (unsigned)R]);
+  auto slot = [&](int j) { return ring + (size_t)(j % R) * SM; };
+
+  if (tid == GT) {
+    // ---- producer ----
+    const long long t0 = prof_issue ? clock64() : 0;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    for (int j = 0; j < total; j++) {
+      if (*(volatile int*)&pp->err) break;
+      // the slot's previous copy of this solve must have been released (copies
+      // of earlier solves were, before those solves ended)
+      if (j >= R && !kkt_wait(&pp->empty[j % R], epar(j - R))) {
+        *(volatile int*)&pp->err = 1;
+        break;
+      }
+      long long el;
+      const T* g = seg(j, el);
+      kkt_bulk_load(slot(j), g, (unsigned)(el * sizeof(T)), &pp->bar[j % R]);
+      *(volatile int*)&pp->issued = j + 1;
+    }
+    if (prof_issue) *prof_issue += (unsigned long long)(clock64() - t0);
+  } else if (tid < GT) {
+    // ---- the solve group ----
+    const bool lo = tid < H;
+    const int r = lo ? tid : tid - H;
+    long long tw = 0, tb = 0;
+    const long long t_start = prof ? clock64() : 0;
+    long long t_fwd = 0;
+    auto sync = [&]() {
+      const long long t = prof ? clock64() : 0;
+      kkt_group_sync(GT);
+      if (prof) tb += clock64() - t;
+    };
+    auto release = [&](int j) {
+      if (tid == 0) kkt_arrive(&pp->empty[j % R]);
+    };
+    // copy j's data: the ring slot, or global memory after a failed wait
+    // (after one failed wait the CTA stops waiting and reads global memory)
+    auto get = [&](int j) -> const T* {
+      long long el;
+      bool ok = !*(volatile int*)&pp->err;
+      if (ok) {
+        const long long t = prof ? clock64() : 0;
+        ok = kkt_wait(&pp->bar[j % R], fpar(j));
+        if (prof) tw += clock64() - t;
+      }
+      if (!ok) {
+        *(volatile int*)&pp->err = 1;
+        atomicMin(&pp->fail, j);
+        return seg(j, el);
+      }
+      return slot(j);
+    };
+    const T* cur = get(0);
+    for (int k = 1; k < nb; k++) {
+      const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+      const int spp = k > 1 ? kv.bs[k - 2] : sp;
+      const T* prev = cur;              // segment k - 1: S_{k-1}^-1 after G_{k-1}
+      cur = get(k);                     // segment k: G_k first
+      if (lo) {
+        if (r < b) c[s0 + r] -= kkt_col_dot(cur, c + sp, b, bp, r);
+      } else {
+        if (r < bp) d[sp + r] = kkt_col_dot(prev + kkt_pad4((long long)bp * (sp - spp)), c + sp, bp, bp, r);
+      }
+      sync();
+      release(k - 1);
+    }
+    {
+      const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
+      const int bp = nb > 1 ? s0 - kv.bs[nb - 2] : 0;
+      if (lo && r < b) d[s0 + r] = kkt_col_dot(cur + kkt_pad4((long long)b * bp), c + s0, b, b, r);
+      sync();
+      release(nb - 1);
+    }
+    if (prof) t_fwd = clock64();
+    for (int t = 0; t + 1 < nb; t++) {
+      const int k = nb - 1 - t;
+      const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+      const T* Gt = get(nb + t);
+      if (lo) {
+        if (r < bp) d[sp + r] -= kkt_col_dot(Gt, d + s0, bp, b, r);
+      } else {
+        if (r < b) xout(kv.perm[s0 + r], d[s0 + r]);
+      }
+      sync();
+      release(nb + t);
+    }
+    for (int i = tid; i < kv.bs[1]; i += GT) xout(kv.perm[i], d[i]);
+    if (prof) {
+      const long long t_end = clock64();
+      prof[0] += (unsigned long long)tw; prof[1] += (unsigned long long)tb;
+      prof[2] += (unsigned long long)(t_fwd - t_start); prof[3] += (unsigned long long)(t_end - t_fwd);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (*(volatile int*)&pp->err) {
+      // copies issued but not waited for land before the CTA goes on; then,
+      // with nothing in flight, the barriers start afresh.  A copy that
+      // still does not land keeps the pipe off for the rest of the kernel.
+      const int iss = *(volatile int*)&pp->issued;
+      bool drained = true;
+      for (int j = pp->fail; j < iss; j++) drained = kkt_wait(&pp->bar[j % R], fpar(j)) && drained;
+      if (drained) {
+        for (int q = 0; q < kKktRingMax; q++) {
+          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(kkt_smem(&pp->bar[q])) : "memory");
+          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(kkt_smem(&pp->empty[q])) : "memory");
+          pp->fph[q] = 0;
+          pp->eph[q] = 0;
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        pp->err = 0;
+      }
+    } else {
+      // every copy of the solve landed and was released
+      for (int q = 0; q < R && q < total; q++) {
+        const unsigned uses = (unsigned)((total - 1 - q) / R + 1);
+        pp->fph[q] += uses;
+        pp->eph[q] += uses;
       }
     }
-  };
-  // pointer to copy j's data: the ring slot, or global memory after a failed wait
-  // (after one failed wait the CTA stops waiting and reads global memory)
-  auto get = [&](int j) -> const T* {
-    const unsigned Q = q0 + (unsigned)j;
-    long long el;
-    if (*(volatile int*)&pp->err) return seg(j, el);
-    const long long t = prof ? clock64() : 0;
-    const bool ok = kkt_wait(&pp->bar[Q % (unsigned)R], (Q / (unsigned)R) & 1u);
-    if (prof) tw += clock64() - t;
-    if (!ok) {
-      *(volatile int*)&pp->err = 1;
-      return seg(j, el);
-    }
-    return slot(j);
-  };
-  issue_upto(R);
-  const T* cur = get(0);
-  for (int k = 1; k < nb; k++) {
-    const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
-    const int spp = k > 1 ? kv.bs[k - 2] : sp;
-    issue_upto(k - 1 + R);            // copies < k - 1 are no longer needed
-    const T* prev = cur;              // segment k - 1: S_{k-1}^-1 after G_{k-1}
-    cur = get(k);                     // segment k: G_k first
-    if (lo) {
-      kkt_block_rows(cur, c + sp, b, bp, 0, half, [&](int r, T a) { c[s0 + r] -= a; });
-    } else {
-      const T* Si = prev + kkt_pad4((long long)bp * (sp - spp));
-      kkt_block_rows(Si, c + sp, bp, bp, half, nt - half, [&](int r, T a) { d[sp + r] = a; });
-    }
-    sync();
+    pp->issued = 0;
+    pp->fail = 0x7fffffff;
   }
-  {
-    const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
-    const int bp = nb > 1 ? s0 - kv.bs[nb - 2] : 0;
-    issue_upto(nb - 1 + R);
-    const T* Si = cur + kkt_pad4((long long)b * bp);
-    kkt_block_rows(Si, c + s0, b, b, 0, nt, [&](int r, T a) { d[s0 + r] = a; });
-    sync();
-  }
-  for (int t = 0; t + 1 < nb; t++) {
-    const int k = nb - 1 - t;
-    const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
-    issue_upto(nb + t + R);           // copies < nb + t are no longer needed
-    const T* GT = get(nb + t);
-    if (lo) {
-      kkt_block_rows(GT, d + s0, bp, b, 0, half, [&](int r, T a) { d[sp + r] -= a; });
-    } else {
-      for (int r = threadIdx.x - half; r < b; r += nt - half) xout(kv.perm[s0 + r], d[s0 + r]);
-    }
-    sync();
-  }
-  for (int r = threadIdx.x; r < kv.bs[1]; r += nt) xout(kv.perm[r], d[r]);
-  if (threadIdx.x == 0) pp->q = q0 + (unsigned)total;
-  sync();
-  if (prof) { prof[0] += (unsigned long long)tw; prof[1] += (unsigned long long)tb; }
+  __syncthreads();
 }
 
-// Solve K x = b with the factor: c holds the permuted right-hand side on entry
-// (c[iperm[i]] = b_i); d is a second permuted n-vector; x (unpermuted) is
-// written through xout(i, value).  All threads of the CTA call it; blockDim.x
-// is a multiple of 64.
+// Solve K x = b with the factor read from global memory: c holds the permuted
+// right-hand side on entry (c[iperm[i]] = b_i); d is a second permuted
+// n-vector; x (unpermuted) is written through xout(i, value).  All threads of
+// the CTA call it; the solve group of kkt_solve_pipe does the block steps.
 template <typename T, typename XO>
 __device__ void kkt_solve(const KktView<T>& kv, T* c, T* d, XO xout) {
-  const int nt = blockDim.x, half = nt >> 1;
-  const bool lo = (int)threadIdx.x < half;
+  const int H = kkt_half(kv.bmax), GT = 2 * H;
+  const int tid = threadIdx.x;
   const int nb = kv.nb;
-  // forward: c_k -= G_k c_{k-1} (lower half) while d_{k-1} = S_{k-1}^-1 c_{k-1} (upper half)
-  for (int k = 1; k < nb; k++) {
-    const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
-    const int spp = k > 1 ? kv.bs[k - 2] : sp;
-    if (lo) {
-      const T* G = kv.F + kv.fo[k];
-      kkt_block_rows(G, c + sp, b, bp, 0, half, [&](int r, T a) { c[s0 + r] -= a; });
-    } else {
-      const T* Si = kv.F + kv.fo[k - 1] + kkt_pad4((long long)bp * (sp - spp));
-      kkt_block_rows(Si, c + sp, bp, bp, half, nt - half, [&](int r, T a) { d[sp + r] = a; });
+  if (tid < GT) {
+    const bool lo = tid < H;
+    const int r = lo ? tid : tid - H;
+    // forward: c_k -= G_k c_{k-1} (lower half) while d_{k-1} = S_{k-1}^-1 c_{k-1} (upper half)
+    for (int k = 1; k < nb; k++) {
+      const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+      const int spp = k > 1 ? kv.bs[k - 2] : sp;
+      if (lo) {
+        if (r < b) c[s0 + r] -= kkt_col_dot(kv.F + kv.fo[k], c + sp, b, bp, r);
+      } else {
+        if (r < bp)
+          d[sp + r] = kkt_col_dot(kv.F + kv.fo[k - 1] + kkt_pad4((long long)bp * (sp - spp)), c + sp, bp, bp, r);
+      }
+      kkt_group_sync(GT);
     }
-    __syncthreads();
-  }
-  {
-    const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
-    const int bp = nb > 1 ? s0 - kv.bs[nb - 2] : 0;
-    kkt_block_rows(kv.F + kv.fo[nb - 1] + kkt_pad4((long long)b * bp), c + s0, b, b, 0, nt,
-                   [&](int r, T a) { d[s0 + r] = a; });
-    __syncthreads();
-  }
-  // backward: x_{k-1} = d_{k-1} - G_k' x_k (lower half) while block k is written out (upper half)
-  for (int k = nb - 1; k >= 1; k--) {
-    const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
-    if (lo) {
-      const T* GT = kv.F + kv.bo[k];
-      kkt_block_rows(GT, d + s0, bp, b, 0, half, [&](int r, T a) { d[sp + r] -= a; });
-    } else {
-      for (int r = threadIdx.x - half; r < b; r += nt - half) xout(kv.perm[s0 + r], d[s0 + r]);
+    {
+      const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
+      const int bp = nb > 1 ? s0 - kv.bs[nb - 2] : 0;
+      if (lo && r < b) d[s0 + r] = kkt_col_dot(kv.F + kv.fo[nb - 1] + kkt_pad4((long long)b * bp), c + s0, b, b, r);
+      kkt_group_sync(GT);
     }
-    __syncthreads();
+    // backward: x_{k-1} = d_{k-1} - G_k' x_k (lower half) while block k is written out (upper half)
+    for (int k = nb - 1; k >= 1; k--) {
+      const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+      if (lo) {
+        if (r < bp) d[sp + r] -= kkt_col_dot(kv.F + kv.bo[k], d + s0, bp, b, r);
+      } else {
+        if (r < b) xout(kv.perm[s0 + r], d[s0 + r]);
+      }
+      kkt_group_sync(GT);
+    }
+    for (int i = tid; i < kv.bs[1]; i += GT) xout(kv.perm[i], d[i]);
   }
-  for (int r = threadIdx.x; r < kv.bs[1]; r += nt) xout(kv.perm[r], d[r]);
   __syncthreads();
 }
 

@@ -55,7 +55,7 @@ constexpr int kKktMergeTo = 32;
 GB_KKT_HD inline long long kkt_pad4(long long e) { return (e + 3) & ~3LL; }
 // Ring slots of the solve's bulk-copy pipeline (0: the solve reads the factor
 // from global memory directly).
-constexpr int kKktRingMax = 4;
+constexpr int kKktRingMax = 16;
 
 // On-chip workspace of the block factorisation (elements): S_{k-1}^-1, S_k,
 // its sweep buffer, K_{k,k-1}, G_k, the assembly tile and its rho values.
@@ -75,9 +75,10 @@ GB_KKT_HD inline long long kkt_ws_elems(int n, int m, int bmax, int segmax, int 
 }
 // Bytes of the whole workspace: the elements above, then copies of the block
 // starts and the forward / backward segment offsets (3 (nb + 1) ints) that
-// every block step reads.
+// every block step reads, and of the permutation and its inverse (2 n ints)
+// that every right-hand side and solution passes through.
 GB_KKT_HD inline long long kkt_ws_bytes(int n, int m, int bmax, int nb, int segmax, int ring, int elem) {
-  return kkt_ws_elems(n, m, bmax, segmax, ring) * elem + 12LL * (nb + 1);
+  return kkt_ws_elems(n, m, bmax, segmax, ring) * elem + 12LL * (nb + 1) + 8LL * n;
 }
 
 struct KktPlan {
@@ -321,6 +322,8 @@ inline int kkt_bmax_limit(int threads, long long ws_bytes, int elem) {
   while (true) {
     const int c = b + 1;
     if ((long long)c * 2 * c > (long long)kKktOutMax * threads) break;
+    // the solve group (two halves of at least c threads, whole warps) and a producer warp
+    if (2 * (c <= 32 ? 32 : ((c + 31) & ~31)) + 32 > threads) break;
     if (kkt_factor_ws_elems(c) * elem > ws_bytes) break;
     b = c;
   }

@@ -85,8 +85,13 @@ struct SolverScalars {
   // DevSettings::profile: SM clock cycles of the last solve, thread 0's view,
   // per phase: 0 right-hand side, 1 linear solve, 2 x / z / y updates,
   // 3 residuals and termination, 4 refactorisation / preconditioner refresh;
-  // of the direct solve: 5 waits for factor segments, 6 block-step barriers
-  unsigned long long prof[7];
+  // of the direct solve: 5 waits for factor segments, 6 block-step barriers,
+  // 7 forward sweep, 8 backward sweep; 9 the sparse product of the
+  // right-hand side, 10 the sparse product of the updates; 11 issuing the
+  // direct solve's bulk copies (the issuing thread's view); counts of direct
+  // solves: 12 all, 13 through the bulk-copy ring, 14 that read the factor
+  // from global memory after a failed wait
+  unsigned long long prof[kProfSlots];
 };
 
 template <typename T>
@@ -569,6 +574,7 @@ struct Solver {
       for_m(g, m, [&](int j) { kw[j] = fma(vec ? pr.rho_vec[j] : rho_s, z[j], -y[j]); });
       __syncthreads();
     }
+    if (prof) { const long long t = clock64(); sc->prof[0] += (unsigned long long)(t - pt); pt = t; }
     rows_rng(g, span_n(g, n), pr.At,
       [&](int j) {
         if (direct) return kw[j];
@@ -587,6 +593,7 @@ struct Solver {
       rows_rng(g, span_m(g, m), pr.A, [&](int c) { return xp[c]; },
         [&](int j, T v) { g.put(pr.t, j, (vec ? pr.rho_vec[j] : rho_s) * v); });
     }
+    if (prof) { const long long t = clock64(); sc->prof[9] += (unsigned long long)(t - pt); pt = t; }
     // time / cancellation ride on this reduction so every CTA sees the same values
     if (g.tid() == 0) {
       mx0[1] = (T)((double)(global_ns() - sc->t_start) * 1e-9);
@@ -624,13 +631,19 @@ struct Solver {
     const double eps = sc->pcg_eps;
 
     if (direct) {
-      // x~ = K^-1 rhs (gb_direct.cuh), written to xp
+      // x~ = K^-1 rhs (gb_direct.cuh), kept on chip (kxs)
       if constexpr (std::is_same<G, BlockGroup>::value) {
-        if (pr.kkt.ring >= 2 && pr.kpipe)
+        const bool piped = pr.kkt.ring >= 2 && pr.kpipe;
+        if (piped)
           kkt_solve_pipe<T>(pr.kkt, pr.kpipe, kc, kc + n, kc + kkt_pad4(2LL * n),
-                            [&](int i, T v) { xp[i] = v; kxs[i] = v; }, prof ? sc->prof + 5 : nullptr);
+                            [&](int i, T v) { kxs[i] = v; }, prof ? sc->prof + 5 : nullptr,
+                            s.profile ? sc->prof + 11 : nullptr);
         else
-          kkt_solve<T>(pr.kkt, kc, kc + n, [&](int i, T v) { xp[i] = v; kxs[i] = v; });
+          kkt_solve<T>(pr.kkt, kc, kc + n, [&](int i, T v) { kxs[i] = v; });
+        if (prof) {
+          sc->prof[12] += 1;
+          if (piped) { sc->prof[13] += 1; if (pr.kpipe->err) sc->prof[14] += 1; }
+        }
       }
     } else {
       const int pcg_it = pcg_core(g, eps, sig, rho_s);
@@ -646,10 +659,11 @@ struct Solver {
     const T al = (T)s.alpha, oma = (T)(1.0 - s.alpha);
     for_n(g, n, [&](int i) {
       const T xo = x[i];
-      const T xn = al * xp[i] + oma * xo;
+      const T xn = al * (direct ? kxs[i] : xp[i]) + oma * xo;
       x[i] = xn;
       pr.dx[i] = xn - xo;
     });
+    if (prof) { const long long t = clock64(); sc->prof[2] += (unsigned long long)(t - pt); pt = t; }
     if (m > 0) {
       rows_rng(g, span_m(g, m), pr.A, [&](int c) { return direct ? kxs[c] : xp[c]; }, [&](int j, T zt) {
         const T ri = vec ? pr.rho_inv_vec[j] : rinv_s;
@@ -664,6 +678,7 @@ struct Solver {
         y[j] = y[j] + d;
       });
     }
+    if (prof) { const long long t = clock64(); sc->prof[10] += (unsigned long long)(t - pt); pt = t; }
     __syncthreads();
     const bool ok = g.sync();
     if (prof) sc->prof[2] += (unsigned long long)(clock64() - pt);
@@ -1224,7 +1239,7 @@ struct Solver {
         sc->t_start = global_ns();
         sc->status = ST_UNSOLVED;
         sc->pcg_iters_total = 0;
-        for (int q = 0; q < 7; q++) sc->prof[q] = 0;
+        for (int q = 0; q < kProfSlots; q++) sc->prof[q] = 0;
       }
     }
     if (it_lo <= 1 && !s.warm_starting) { cold_start(g); }

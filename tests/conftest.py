@@ -27,6 +27,13 @@ def oracle_lib():
     return Library(path, 64)
 
 
+def reference_dir():
+    """Location of the reference sources as oracle/Makefile resolves it
+    (OSQP_REFERENCE_DIR overrides), or "" when they are absent."""
+    r = subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "refdir"], capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
 @pytest.fixture(scope="session")
 def ref_tests():
     return np.load(os.path.join(GOLDEN, "ref_tests.npz"))

