@@ -91,8 +91,9 @@ def make_workload(count, steps, seed=3, share=0):
 # DRAM bytes per algorithmic byte of the solve launch, from one ncu capture
 # of a smaller batch of the same QPs (the 4096-QP launch is too long to
 # capture); the launch's traffic is this ratio times its algorithmic bytes.
-# PCG path: 304 QPs, 52.2 + 7.0 GB DRAM for 285.6 GB algorithmic.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {2: (52.202385 + 6.987452) / 285.586664900, 1: None}
+# Direct solver, FP64: 304 QPs, 89.39 + 12.51 GB DRAM for 108.06 GB
+# algorithmic.  The PCG path and the FP32 direct path are not captured.
+TRAFFIC_PER_ALGORITHMIC_BYTE = {("direct", "f64"): (89.385127 + 12.505955) / 108.057547680}
 
 
 def measured_peak():
@@ -472,11 +473,17 @@ def _oracle_job(args_):
 
 
 def single_config(args):
+    print(json.dumps(single_config_result(args.config, args.oracle_timeout)))
+
+
+def single_config_result(which, oracle_timeout):
+    """One single-QP configuration on GPU 0 (FP32 and FP64 paths) and, within
+    oracle_timeout seconds, the FP64 CPU oracle."""
     import torch
     from osqp_gb300 import load
     from osqp_gb300.api import OSQP, DIRECT_SOLVER, INDIRECT_SOLVER
     torch.cuda.set_device(0)
-    if args.config == "large_sparse":
+    if which == "large_sparse":
         data = pb.large_sparse()
         st = dict(SETTINGS, warm_starting=0, polishing=0, linsys_solver=INDIRECT_SOLVER)
         oracle_linsys = INDIRECT_SOLVER
@@ -516,7 +523,7 @@ def single_config(args):
                          "frac": byt / (kms * 1e-3) / 1e9 / peak, "peak_source": peak_kind},
             "obj": obj, "prim_res": prim, "dual_res": dual}
         solver.cleanup()
-    if args.oracle_timeout > 0:
+    if oracle_timeout > 0:
         lib_path = os.path.join(REPO, "oracle", "_build", "liboracle.so")
         if not os.path.exists(lib_path):
             subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "port"], check=True)
@@ -524,7 +531,7 @@ def single_config(args):
         with ctx.Pool(1) as pool:
             job = pool.apply_async(_oracle_job, ((lib_path, data, st, oracle_linsys),))
             try:
-                secs, xo, yo, status, it, spol = job.get(timeout=args.oracle_timeout)
+                secs, xo, yo, status, it, spol = job.get(timeout=oracle_timeout)
                 obj, prim, dual = _host_residuals(data, xo, yo)
                 out["oracle"] = {"kind": "direct LDL^T (builtin)" if oracle_linsys == DIRECT_SOLVER else
                                  "reduced-KKT PCG (FP64 restatement of the CUDA backend)", "status": status,
@@ -533,17 +540,20 @@ def single_config(args):
                 for prec, pth in out["paths"].items():
                     pth["obj_rel_err_vs_oracle"] = abs(pth["obj"] - obj) / max(1.0, abs(obj))
             except mp.TimeoutError:
-                out["oracle"] = {"unavailable": f"FP64 CPU oracle did not finish within {args.oracle_timeout:.0f} s"}
+                out["oracle"] = {"unavailable": f"FP64 CPU oracle did not finish within {oracle_timeout:.0f} s"}
                 pool.terminate()
     ref = out["paths"]["f64"]["obj"]
     out["paths"]["f32"]["obj_rel_err_vs_f64_gpu"] = abs(out["paths"]["f32"]["obj"] - ref) / max(1.0, abs(ref))
-    print(json.dumps(out))
+    if oracle_timeout <= 0:
+        out["oracle"] = {"unavailable": "not run in this invocation (python bench.py --config " + which +
+                                        " runs it, with --oracle-timeout seconds)"}
+    return out
 
 
 # ---------------------------------------------------------------------------
 # Served form: Poisson request stream over resident pools (continuous batching)
 # ---------------------------------------------------------------------------
-def serve_leg(args):
+def serve_leg(args, rate=None, seconds=None):
     """50% MPC and 50% factor-model portfolio requests from `streams` recurring
     problems each, Poisson arrivals at `rate` req/s for `seconds`.  Each
     stream's data drift between its requests: an MPC stream's measured state
@@ -570,8 +580,10 @@ def serve_leg(args):
     pid = [srv.add_pool(b) for b in pools]
     nxs = [_nx_of(p[2]) for p in mpc]
     rg = np.random.default_rng([11, 3])
-    n_req = int(args.serve_rate * args.serve_seconds)
-    t_arr = np.cumsum(rg.exponential(1.0 / args.serve_rate, n_req))
+    rate = args.serve_rate if rate is None else rate
+    seconds = args.serve_seconds if seconds is None else seconds
+    n_req = int(rate * seconds)
+    t_arr = np.cumsum(rg.exponential(1.0 / rate, n_req))
     kind = rg.integers(0, 2, n_req)
     which = rg.integers(0, S, n_req)
     payload = []
@@ -615,7 +627,7 @@ def serve_leg(args):
     for b in pools:
         b.cleanup()
     mk = kind == 0
-    return {"rate_rps": args.serve_rate, "seconds": args.serve_seconds, "requests": n_req,
+    return {"rate_rps": rate, "seconds": seconds, "requests": n_req, "drained_s": elapsed,
             "streams": {"mpc": S, "portfolio": S}, "concurrency": args.serve_concurrency,
             "solves_per_s": n_req / elapsed, "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "p50_ms_mpc": float(np.percentile(lat[mk], 50)),
@@ -637,6 +649,8 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="served form: Poisson arrivals (req/s); 0 = skip")
     ap.add_argument("--serve-seconds", type=float, default=6.0)
+    ap.add_argument("--serve-config-rate", type=float, default=2000.0,
+                    help="served form: also one second of Poisson arrivals at this rate (0 = skip)")
     ap.add_argument("--serve-streams", type=int, default=128, help="recurring problems per class")
     ap.add_argument("--serve-concurrency", type=int, default=32, help="launches in flight")
     ap.add_argument("--config", default="mpc_batch", choices=["mpc_batch", "large_sparse", "svm"])
@@ -654,6 +668,10 @@ def main():
     ap.add_argument("--precision", default="f64", choices=["f64", "f32"],
                     help="arithmetic of the measured batched solve (f64: the builtin algorithm's trajectory; "
                          "f32: FP32 iterates and factor with double-float reductions)")
+    ap.add_argument("--single-configs", type=int, default=1,
+                    help="also run the large sparse QP and the SVM (single-QP configurations) as extra keys")
+    ap.add_argument("--large-sparse-oracle-timeout", type=float, default=180.0,
+                    help="seconds allowed for the FP64 oracle of the large sparse QP in the default run")
     ap.add_argument("--other-precision", type=int, default=1,
                     help="also time one step in the other precision, with its parity")
     args = ap.parse_args()
@@ -705,6 +723,13 @@ def main():
     other = "f32" if args.precision == "f64" else "f64"
     leg2 = precision_leg(other, probs, ls, us, W) if (direct and args.other_precision) else None
     served = serve_leg(args) if args.serve_rate > 0 else None
+    # the serving configuration's lowest arrival rate, one second of arrivals
+    served_cfg = serve_leg(args, args.serve_config_rate, 1.0) if args.serve_config_rate > 0 else None
+    # the two single-QP configurations, as extra keys of this line
+    singles = {}
+    if args.single_configs:
+        singles["large_sparse"] = single_config_result("large_sparse", args.large_sparse_oracle_timeout)
+        singles["svm"] = single_config_result("svm", 0)
     peak, peak_kind = measured_peak()
     sizes_m = [p[2].shape[0] for p in probs]
     # the FP64 oracle on the host cores: every QP, through the warm-up steps
@@ -714,7 +739,7 @@ def main():
     if leg2 is not None:
         first2 = leg2.pop("first")
         leg2["parity_vs_fp64_oracle"] = parity(first2, cpu, len(probs)) if cpu else None
-    tr = TRAFFIC_PER_ALGORITHMIC_BYTE[SETTINGS["linsys_solver"]]
+    tr = TRAFFIC_PER_ALGORITHMIC_BYTE.get(("direct" if direct else "indirect", args.precision))
     line = dict(
         metric=metric, value=g["value"], unit="solves/s", n_gpus=world, steps=K, warmup=W,
         ms_per_step=g["ms_per_step"], higher_is_better=True, scaling="weak", vs_baseline=None,
@@ -741,7 +766,8 @@ def main():
         other_precision=leg2,
         indirect=indirect,
         spmv_tile_entries_per_lane=g["tile"],
-        served=served,
+        served=served, served_at_config_rate=served_cfg,
+        **singles,
     )
     print(json.dumps(line))
 
