@@ -564,15 +564,16 @@ def serve_leg(args, rate=None, seconds=None):
     import threading
     from osqp_gb300 import load
     from osqp_gb300.api import Batch, Server
-    lib = load("f32")
+    lib = load(args.precision)
     S = args.serve_streams
     mpc = pb.mpc_batch(S, seed=11)
     port = [pb.portfolio(seed=20000 + i) for i in range(S)]
     st = dict(SETTINGS, warm_starting=1)
     pools = []
-    # MPC requests take the configured solver; portfolio QPs (a budget row over
-    # every asset: one dense block) always take the PCG
-    for probs, ls_ in ((mpc, SETTINGS["linsys_solver"]), (port, 2)):
+    # both classes take the configured solver: MPC QPs the block-tridiagonal
+    # direct solve, portfolio QPs (a budget row and factor rows over every
+    # asset) its diagonal-plus-dense-rows form
+    for probs, ls_ in ((mpc, SETTINGS["linsys_solver"]), (port, SETTINGS["linsys_solver"])):
         b = Batch(lib)
         assert b.setup(probs, **dict(st, linsys_solver=ls_)) == 0, "pool set-up refused"
         pools.append(b)
@@ -593,10 +594,10 @@ def serve_leg(args, rate=None, seconds=None):
             P, q, A, l, u = mpc[i]
             x0[i] = np.clip(x0[i] + 0.05 * rg.standard_normal(nxs[i]), -1.0, 1.0)
             l2, u2 = pb.mpc_x0_bounds(l, u, x0[i])
-            payload.append((pid[0], int(i), None, l2.astype(np.float32), u2.astype(np.float32), P.shape[0]))
+            payload.append((pid[0], int(i), None, l2, u2, P.shape[0]))
         else:
             P, q, A, l, u = port[i]
-            q2 = (q * (1.0 + 0.02 * rg.standard_normal(q.size))).astype(np.float32)
+            q2 = q * (1.0 + 0.02 * rg.standard_normal(q.size))
             payload.append((pid[1], int(i), q2, None, None, P.shape[0]))
     # warm-up: one request per stream (cold start of every stream), untimed
     for j, probs in enumerate((mpc, port)):

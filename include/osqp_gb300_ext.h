@@ -168,6 +168,16 @@ OSQPInt osqp_gb300_batch_rho_updates(OSQPBatch* batch, OSQPInt* rho_updates);
  * width.  No reference counterpart. */
 OSQPInt osqp_gb300_batch_factor_elems(OSQPBatch* batch, long long* elems);
 
+/* Direct solver in the diagonal-plus-dense-rows form (a QP whose constraint
+ * rows couple too many variables for the block-tridiagonal ordering, with a
+ * diagonal P): for QP k of a batch, *r = its dense rows (rows of A with two or
+ * more entries; 0 when the QP uses the block form or the PCG), and, where the
+ * pointers are not NULL, the rows (r entries), the inverse capacitance matrix
+ * (R_d^-1 + A_d Dg^-1 A_d')^-1 (r x r, row-major) and Dg^-1 (n entries) of the
+ * scaled problem for the current rho.  No reference counterpart. */
+OSQPInt osqp_gb300_batch_dense_rows(OSQPBatch* batch, OSQPInt k, OSQPInt* r, OSQPInt* rows, OSQPFloat* cinv,
+                                    OSQPFloat* dginv);
+
 OSQPInt osqp_gb300_batch_cleanup(OSQPBatch* batch);
 
 /* Ordering of the direct solver for one QP (host memory; no device work):

@@ -473,6 +473,25 @@ class Batch:
                          "direct_solves", "direct_solves_ring", "direct_solves_global", "unused"],
                         out.tolist()))
 
+    def dense_rows(self, k: int):
+        """Dense-row form of QP k (osqp_gb300_batch_dense_rows): (rows, C^-1, Dg^-1),
+        or None when QP k does not use that form."""
+        L, I, F = self.L.lib, self.L.I, self.L.F
+        r = I()
+        rc = L.osqp_gb300_batch_dense_rows(self._h, k, C.byref(r), None, None, None)
+        if rc:
+            raise RuntimeError(f"osqp_gb300_batch_dense_rows failed: {rc}")
+        if r.value == 0:
+            return None
+        n = int(self.packed["n"][k])
+        rows = np.zeros(r.value, np.int32)
+        cinv = np.zeros(r.value * r.value, self.L.np_float)
+        dginv = np.zeros(n, self.L.np_float)
+        rc = L.osqp_gb300_batch_dense_rows(self._h, k, C.byref(r), _ptr(rows, I), _ptr(cinv, F), _ptr(dginv, F))
+        if rc:
+            raise RuntimeError(f"osqp_gb300_batch_dense_rows failed: {rc}")
+        return rows, cinv.reshape(r.value, r.value), dginv
+
     def factor_elems(self):
         """Elements of each QP's direct-solver factor (0 with the indirect solver)."""
         out = np.zeros(self.count, np.int64)

@@ -75,6 +75,10 @@ struct BatchInst {
   int knb, kbmax, kb_off, kcr_off;
   int kring, ksegmax;   // bulk-copy ring slots of the solve and largest factor segment
   long long kf_off;
+  // diagonal-plus-dense-rows form (kdr > 0; knb == 0): dense rows, offset of
+  // the QP's dense-row list and of its inverse capacitance matrix
+  int kdr, kdr_off;
+  long long kc_off;
 };
 
 template <typename TT>
@@ -92,6 +96,8 @@ struct BatchArrays {
   // direct KKT solve: plans and factors of every QP (gb_kkt_plan.h)
   int *kperm, *kiperm, *kbs, *kfo, *kbo, *kco, *kcr;
   TT* kF;
+  int *kdrows, *kdidx;  // dense-row lists, row -> dense-row maps (msum)
+  TT *kCinv, *kDginv;   // inverse capacitance matrices, Dg^-1 (nsum)
 
   __device__ DevProblem<TT> problem(int k) const {
     const BatchInst b = inst[k];
@@ -124,6 +130,12 @@ struct BatchArrays {
       pr.kkt.cr = kcr + b.kcr_off;
       pr.kkt.perm = kperm + o; pr.kkt.iperm = kiperm + o;
       pr.kkt.F = kF + b.kf_off;
+    } else if (b.kdr > 0) {
+      pr.kkt.dr = b.kdr;
+      pr.kkt.drows = kdrows + b.kdr_off;
+      pr.kkt.didx = kdidx + p;
+      pr.kkt.Cinv = kCinv + b.kc_off;
+      pr.kkt.Dginv = kDginv + o;
     }
     return pr;
   }
@@ -308,13 +320,17 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   bool staged = false;
   // direct KKT solve: the dynamic shared memory is the factorisation's and the
   // block solve's workspace (the QP's data stay in HBM / L2)
-  const bool direct = pv.kkt.nb > 0;
+  const bool direct = kkt_direct(pv.kkt);
   if (direct) {
     pv.kws = (TT*)dsm;
     pv.kpipe = kpipe;
-    if (!kpipe) pv.kkt.ring = 0;
-    kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.m, pv.kkt.bmax, pv.kkt.segmax, pv.kkt.ring) * sizeof(TT)),
-                     pv.n);
+    if (pv.kkt.dr > 0) {
+      dr_on_chip(pv.kkt, (int*)(dsm + dr_ws_elems(pv.n, pv.m, pv.kkt.dr) * sizeof(TT)), pv.m);
+    } else {
+      if (!kpipe) pv.kkt.ring = 0;
+      kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.m, pv.kkt.bmax, pv.kkt.segmax, pv.kkt.ring) * sizeof(TT)),
+                       pv.n);
+    }
     __syncthreads();
   }
   if (mode == kModeSolve && dsm_bytes > 0 && !direct) {
@@ -631,6 +647,7 @@ struct OSQPBatch_ {
   int count, device;
   int direct;             // linsys_solver = direct: every QP has a KKT plan
   long long kf_total;     // direct: factor elements of the whole batch
+  long long kc_total;     // direct, dense-row form: inverse capacitance elements of the whole batch
   long long nsum, msum, nnzT, nnzA, nnzPf;
   size_t binv_elems;    // block-Jacobi storage (0 unless cg_precond = 2)
   cudaStream_t stream;
@@ -873,7 +890,8 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   b->direct = st.linsys_solver == OSQP_DIRECT_SOLVER;
   const int cap_kib0 = env_int("OSQP_GB300_BATCH_SMEM_KIB", -1);
   std::vector<KktPlan> plans;
-  long long kb_tot = 0, kcr_tot = 0, kf_tot = 0;
+  std::vector<DrPlan> drplans;
+  long long kb_tot = 0, kcr_tot = 0, kf_tot = 0, kdr_tot = 0, kc_tot = 0;
   if (b->direct) {
     // the factorisation and the block solve work in the CTA's shared memory
     int minb0 = 1;
@@ -883,6 +901,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     std::vector<OSQPInt> hAi(ao > 0 ? ao : 1);
     if (ao && cudaMemcpy(hAi.data(), Ai, sizeof(OSQPInt) * ao, cudaMemcpyDefault) != cudaSuccess) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
     plans.resize(count);
+    drplans.resize(count);
     std::vector<int> prc(count, 0), ring(count, 0);
     const int nthr = std::max(1, std::min((int)std::thread::hardware_concurrency(), std::min(count, 64)));
     std::vector<std::thread> pool;
@@ -892,6 +911,21 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
           const BatchInst& I = b->inst[k];
           prc[k] = kkt_plan_build(I.n, I.m, hPp.data() + pp_off[k], hPi.data() + I.pt_off, hAp.data() + pp_off[k],
                                   hAi.data() + I.a_off, blim, plans[k]);
+          if (prc[k] == 1 && sizeof(T) == 8) {
+            // no block ordering within the limit: the diagonal-plus-dense-rows
+            // form, with as many dense rows as its workspace allows.  FP64
+            // build only: with FP32 iterates its solves left factor-model
+            // portfolios at 1.5-8x the builtin's ADMM iterations (some not
+            // converging), so the FP32 build keeps the PCG for such QPs
+            int rmax = 0;
+            while (rmax < kDrMaxRows && dr_ws_bytes(I.n, I.m, rmax + 1, (int)sizeof(T)) <= b->dsm) rmax++;
+            if (!dr_plan_build(I.n, I.m, hPp.data() + pp_off[k], hPi.data() + I.pt_off, hAp.data() + pp_off[k],
+                               hAi.data() + I.a_off, rmax, drplans[k])) {
+              prc[k] = 0;
+              plans[k] = KktPlan();
+              continue;
+            }
+          }
           if (!prc[k]) {
             // ring slots of the solve's bulk-copy pipeline: as many as fit (at least 2), else none
             int R = kKktRingMax;
@@ -915,17 +949,21 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
         return OSQP_LINSYS_SOLVER_INIT_ERROR;
       }
       BatchInst& I = b->inst[k];
+      I.kdr = drplans[k].r; I.kdr_off = (int)kdr_tot; I.kc_off = kc_tot;
+      kdr_tot += drplans[k].r; kc_tot += (long long)drplans[k].r * drplans[k].r;
       I.knb = plans[k].nb; I.kbmax = plans[k].bmax;
       I.kring = env_int("OSQP_GB300_KKT_RING", 1) ? ring[k] : 0; I.ksegmax = plans[k].segmax;
       I.kb_off = (int)kb_tot; I.kcr_off = (int)kcr_tot; I.kf_off = kf_tot;
-      kb_tot += plans[k].nb + 1; kcr_tot += (long long)plans[k].cr.size(); kf_tot += plans[k].fsize;
+      if (I.kdr == 0) { kb_tot += plans[k].nb + 1; kcr_tot += (long long)plans[k].cr.size(); kf_tot += plans[k].fsize; }
     }
     if (kb_tot > INT32_MAX || kcr_tot > INT32_MAX) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
     b->kf_total = kf_tot;
+    b->kc_total = kc_tot;
   } else {
     for (int k = 0; k < count; k++) {
       BatchInst& I = b->inst[k];
       I.knb = 0; I.kbmax = 0; I.kb_off = 0; I.kcr_off = 0; I.kf_off = 0; I.kring = 0; I.ksegmax = 0;
+      I.kdr = 0; I.kdr_off = 0; I.kc_off = 0;
     }
   }
 
@@ -955,6 +993,8 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   size_t o_kbs = pl.take(sizeof(int) * kb_tot), o_kfo = pl.take(sizeof(int) * kb_tot), o_kco = pl.take(sizeof(int) * kb_tot);
   size_t o_kbo = pl.take(sizeof(int) * kb_tot);
   size_t o_kcr = pl.take(sizeof(int) * kcr_tot), o_kF = pl.take(sizeof(T) * kf_tot);
+  size_t o_kdrows = pl.take(sizeof(int) * kdr_tot), o_kdidx = pl.take(sizeof(int) * (kdr_tot ? msum : 0));
+  size_t o_kCinv = pl.take(sizeof(T) * kc_tot), o_kDginv = pl.take(sizeof(T) * (kdr_tot ? nsum : 0));
   {
     // admission by free device memory: refuse (rather than fail part-way)
     // when the pool and the set-up scratch would not fit
@@ -982,6 +1022,8 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   B.kbs = (int*)(a + o_kbs); B.kfo = (int*)(a + o_kfo); B.kco = (int*)(a + o_kco); B.kcr = (int*)(a + o_kcr);
   B.kbo = (int*)(a + o_kbo);
   B.kF = (T*)(a + o_kF);
+  B.kdrows = (int*)(a + o_kdrows); B.kdidx = (int*)(a + o_kdidx);
+  B.kCinv = (T*)(a + o_kCinv); B.kDginv = (T*)(a + o_kDginv);
   b->d_inst = (BatchInst*)(a + o_inst); B.inst = b->d_inst;
   b->d_order = (int*)(a + o_order);
   b->d_queue = (int*)(a + o_misc); b->d_flag = b->d_queue + 1;
@@ -1007,6 +1049,11 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     kcr_h.reserve(kcr_tot);
     for (int k = 0; k < count; k++) {
       const KktPlan& q = plans[k];
+      if (q.perm.empty()) {
+        // a QP of the dense-row form: no permutation, its slots keep their place
+        kperm_h.insert(kperm_h.end(), b->inst[k].n, 0);
+        kiperm_h.insert(kiperm_h.end(), b->inst[k].n, 0);
+      }
       kperm_h.insert(kperm_h.end(), q.perm.begin(), q.perm.end());
       kiperm_h.insert(kiperm_h.end(), q.iperm.begin(), q.iperm.end());
       kbs_h.insert(kbs_h.end(), q.bs.begin(), q.bs.end());
@@ -1017,12 +1064,25 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     }
     BT_TRY(cudaMemcpyAsync(B.kperm, kperm_h.data(), sizeof(int) * nsum, cudaMemcpyHostToDevice, s));
     BT_TRY(cudaMemcpyAsync(B.kiperm, kiperm_h.data(), sizeof(int) * nsum, cudaMemcpyHostToDevice, s));
-    BT_TRY(cudaMemcpyAsync(B.kbs, kbs_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
-    BT_TRY(cudaMemcpyAsync(B.kfo, kfo_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
-    BT_TRY(cudaMemcpyAsync(B.kbo, kbo_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
-    BT_TRY(cudaMemcpyAsync(B.kco, kco_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
+    if (kb_tot) BT_TRY(cudaMemcpyAsync(B.kbs, kbs_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
+    if (kb_tot) BT_TRY(cudaMemcpyAsync(B.kfo, kfo_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
+    if (kb_tot) BT_TRY(cudaMemcpyAsync(B.kbo, kbo_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
+    if (kb_tot) BT_TRY(cudaMemcpyAsync(B.kco, kco_h.data(), sizeof(int) * kb_tot, cudaMemcpyHostToDevice, s));
     if (kcr_tot) BT_TRY(cudaMemcpyAsync(B.kcr, kcr_h.data(), sizeof(int) * kcr_tot, cudaMemcpyHostToDevice, s));
     plans.clear();
+    if (kdr_tot) {
+      std::vector<int> drows_h, didx_h(msum, -1);
+      drows_h.reserve(kdr_tot);
+      for (int k = 0; k < count; k++) {
+        const DrPlan& q = drplans[k];
+        drows_h.insert(drows_h.end(), q.rows.begin(), q.rows.end());
+        for (int a2 = 0; a2 < q.r; a2++) didx_h[b->inst[k].m_off + q.rows[a2]] = a2;
+      }
+      BT_TRY(cudaMemcpyAsync(B.kdrows, drows_h.data(), sizeof(int) * kdr_tot, cudaMemcpyHostToDevice, s));
+      BT_TRY(cudaMemcpyAsync(B.kdidx, didx_h.data(), sizeof(int) * msum, cudaMemcpyHostToDevice, s));
+      BT_TRY(cudaStreamSynchronize(s));   // the host vectors go out of scope
+    }
+    drplans.clear();
   }
 
   // ---- device structure build ----
@@ -1254,6 +1314,15 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
       fo += fsl[i].second;
     }
   }
+  // and the dense-row form's inverse capacitance matrices and Dg^-1
+  T* csnap = nullptr;
+  if (!rc && b->kc_total > 0) {
+    if (cudaMallocAsync((void**)&csnap, sizeof(T) * (size_t)(b->kc_total + b->nsum), s) != cudaSuccess) rc = OSQP_MEM_ALLOC_ERROR;
+    else {
+      cudaMemcpyAsync(csnap, B.kCinv, sizeof(T) * b->kc_total, cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(csnap + b->kc_total, B.kDginv, sizeof(T) * b->nsum, cudaMemcpyDeviceToDevice, s);
+    }
+  }
   LaunchBufs lb{dbuf, ns, dbuf + 2 * (size_t)ns, dbuf + ns};
   float best_ms = 1e30f, default_ms = 1e30f;
   for (int cand : {kDefaultPerLane, 4, 16}) {
@@ -1297,6 +1366,11 @@ extern "C" OSQPInt osqp_gb300_batch_autotune(OSQPBatch* b, OSQPInt probe_iter, O
       fo += fsl[i].second;
     }
     cudaFreeAsync(fsnap, s);
+  }
+  if (csnap) {
+    cudaMemcpyAsync(B.kCinv, csnap, sizeof(T) * b->kc_total, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(B.kDginv, csnap + b->kc_total, sizeof(T) * b->nsum, cudaMemcpyDeviceToDevice, s);
+    cudaFreeAsync(csnap, s);
   }
   if (dbuf) cudaFreeAsync(dbuf, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) rc = OSQP_ALGEBRA_LOAD_ERROR;
@@ -1396,6 +1470,25 @@ extern "C" OSQPInt osqp_gb300_batch_factor_elems(OSQPBatch* b, long long* elems)
   if (!b || !elems) return OSQP_WORKSPACE_NOT_INIT_ERROR;
   for (int k = 0; k < b->count; k++)
     elems[k] = b->direct ? ((k + 1 < b->count ? b->inst[k + 1].kf_off : b->kf_total) - b->inst[k].kf_off) : 0;
+  return 0;
+}
+
+extern "C" OSQPInt osqp_gb300_batch_dense_rows(OSQPBatch* b, OSQPInt k, OSQPInt* r, OSQPInt* rows, OSQPFloat* cinv,
+                                               OSQPFloat* dginv) {
+  if (!b || k < 0 || k >= b->count || !r) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  const BatchInst& I = b->inst[k];
+  *r = b->direct ? I.kdr : 0;
+  if (!*r) return 0;
+  cudaStream_t s = b->stream;
+  if (rows) {
+    std::vector<int> h(I.kdr);
+    BT_TRY(cudaMemcpyAsync(h.data(), b->B.kdrows + I.kdr_off, sizeof(int) * I.kdr, cudaMemcpyDeviceToHost, s));
+    BT_TRY(cudaStreamSynchronize(s));
+    for (int a = 0; a < I.kdr; a++) rows[a] = h[a];
+  }
+  if (cinv) BT_TRY(cudaMemcpyAsync(cinv, b->B.kCinv + I.kc_off, sizeof(T) * (size_t)I.kdr * I.kdr, cudaMemcpyDefault, s));
+  if (dginv) BT_TRY(cudaMemcpyAsync(dginv, b->B.kDginv + I.n_off, sizeof(T) * I.n, cudaMemcpyDefault, s));
+  BT_TRY(cudaStreamSynchronize(s));
   return 0;
 }
 

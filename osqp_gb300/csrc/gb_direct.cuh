@@ -54,7 +54,17 @@ struct KktView {
   const int* perm = nullptr;     // permuted position -> variable
   const int* iperm = nullptr;    // variable -> permuted position
   T* F = nullptr;                // factor
+  // diagonal-plus-dense-rows form (gb_kkt_plan.h; dr == 0 otherwise)
+  int dr = 0;                    // dense rows r
+  const int* drows = nullptr;    // [r] rows of A with two or more entries
+  const int* didx = nullptr;     // [m] position of a row of A in drows, -1 for the others
+  T* Cinv = nullptr;             // [r r] (R_d^-1 + A_d Dg^-1 A_d')^-1, row-major
+  T* Dginv = nullptr;            // [n] 1 / Dg
 };
+
+// A direct solve of either form is set up.
+template <typename T>
+__host__ __device__ inline bool kkt_direct(const KktView<T>& kv) { return kv.nb > 0 || kv.dr > 0; }
 
 // Factor K = P + sigma I + A' R A (scaled data) into F.  ws: on-chip
 // workspace of kkt_factor_ws_elems(bmax) elements.  rho_vec == nullptr: the
@@ -533,6 +543,106 @@ __device__ void kkt_solve(const KktView<T>& kv, T* c, T* d, XO xout) {
     for (int i = tid; i < kv.bs[1]; i += GT) xout(kv.perm[i], d[i]);
   }
   __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal-plus-dense-rows form (gb_kkt_plan.h)
+// ---------------------------------------------------------------------------
+
+// Copy the dense-row list and the row map to on-chip memory `dst` (r + m ints).
+template <typename T>
+__device__ __forceinline__ void dr_on_chip(KktView<T>& kv, int* dst, int m) {
+  int* rows = dst;
+  int* didx = dst + kv.dr;
+  for (int k = threadIdx.x; k < kv.dr; k += blockDim.x) rows[k] = kv.drows[k];
+  for (int j = threadIdx.x; j < m; j += blockDim.x) didx[j] = kv.didx[j];
+  kv.drows = rows;
+  kv.didx = didx;
+}
+
+// Dg^-1 and C^-1 for the current rho (scaled data).  C is formed and inverted
+// in place in kv.Cinv (global memory, L2-resident: r r elements); ws: on-chip
+// workspace of n elements.  Returns false when Dg or C has a pivot that is
+// not positive (K not positive definite).  All threads of the CTA call it;
+// every entry has one owner and a fixed summation order.
+template <typename T>
+__device__ __noinline__ bool dr_factor(const KktView<T>& kv, int n, const CSR<T>& P, const CSR<T>& A,
+                                       const CSR<T>& At, const T* rho_vec, T rho_s, T sigma, T* ws) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  const int r = kv.dr;
+  T* C = kv.Cinv;
+  T* sv = ws;
+  __shared__ int s_bad;
+  if (tid == 0) s_bad = 0;
+  __syncthreads();
+  // Dg = P_ii + sigma + the single-entry rows' rho a^2: one warp per variable
+  for (int i = warp; i < n; i += nwarps) {
+    T pdiag = T(0), dsum = T(0);
+    for (int e = P.rowptr[i] + lane; e < P.rowptr[i + 1]; e += 32)
+      if (P.col[e] == i) pdiag = P.val[e];
+    for (int e = At.rowptr[i] + lane; e < At.rowptr[i + 1]; e += 32) {
+      const int row = At.col[e];
+      if (kv.didx[row] < 0) {
+        const T a = At.val[e];
+        dsum += (a * a) * (rho_vec ? rho_vec[row] : rho_s);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+      pdiag += __shfl_xor_sync(0xffffffffu, pdiag, o);   // one lane holds it
+    }
+    if (lane == 0) {
+      const T d = (pdiag + sigma) + dsum;
+      if (!(d > T(0)) || !isfinite((double)d)) s_bad = 1;
+      kv.Dginv[i] = T(1) / d;
+    }
+  }
+  __syncthreads();
+  if (s_bad) return false;
+  // C = R_d^-1 + A_d Dg^-1 A_d': row a of A_d scaled by Dg^-1 is scattered into
+  // sv, then every C_ab (b >= a) is one warp's dot of row b with it
+  for (int i = tid; i < n; i += nt) sv[i] = T(0);
+  __syncthreads();
+  for (int a = 0; a < r; a++) {
+    const int ra = kv.drows[a];
+    for (int e = A.rowptr[ra] + tid; e < A.rowptr[ra + 1]; e += nt) sv[A.col[e]] = A.val[e] * kv.Dginv[A.col[e]];
+    __syncthreads();
+    for (int b = a + warp; b < r; b += nwarps) {
+      const int rb = kv.drows[b];
+      Acc<T> acc;   // double-float in the FP32 build: a dense row sums many entries
+      for (int e = A.rowptr[rb] + lane; e < A.rowptr[rb + 1]; e += 32) acc.add_prod(A.val[e], sv[A.col[e]]);
+      warp_accT(acc);
+      if (lane == 0) {
+        double c = acc.value();
+        if (b == a) c += 1.0 / (double)(rho_vec ? rho_vec[ra] : rho_s);
+        C[(size_t)a * r + b] = (T)c;
+        C[(size_t)b * r + a] = (T)c;
+      }
+    }
+    __syncthreads();
+    for (int e = A.rowptr[ra] + tid; e < A.rowptr[ra + 1]; e += nt) sv[A.col[e]] = T(0);
+    __syncthreads();
+  }
+  // in-place symmetric sweeps (C stays exactly symmetric): -C^-1 after r sweeps
+  for (int k = 0; k < r; k++) {
+    const T piv = C[(size_t)k * r + k];
+    if (!(piv > T(0)) || !isfinite((double)piv)) return false;   // CTA-uniform
+    const T d = T(1) / piv;
+    for (int o = tid; o < r * r; o += nt) {
+      const int i = o / r, j = o - i * r;
+      if (i != k && j != k) C[o] -= (C[(size_t)i * r + k] * C[(size_t)k * r + j]) * d;
+    }
+    __syncthreads();
+    for (int o = tid; o < r; o += nt)
+      if (o != k) { C[(size_t)o * r + k] *= d; C[(size_t)k * r + o] *= d; }
+    if (tid == 0) C[(size_t)k * r + k] = -d;
+    __syncthreads();
+  }
+  for (int o = tid; o < r * r; o += nt) C[o] = -C[o];
+  __syncthreads();
+  return true;
 }
 
 }  // namespace gb

@@ -330,4 +330,66 @@ inline int kkt_bmax_limit(int threads, long long ws_bytes, int elem) {
   return b;
 }
 
+// ---------------------------------------------------------------------------
+// Diagonal-plus-dense-rows form (Woodbury).  When the block ordering does not
+// apply -- a row of A couples most variables, as a budget row or the factor
+// rows of a factor model do -- but P is diagonal, K splits into a diagonal and
+// the rows of A with two or more entries ("dense rows"):
+//   K = Dg + A_d' R_d A_d,   Dg = diag(P) + sigma + sum over single-entry rows
+//                                  of rho_j a_j^2,
+// and the builtin's quasi-definite KKT system restricted to the dense rows is
+// solved by eliminating x:  C nu = A_d Dg^-1 b_s - (z_d - R_d^-1 y_d),
+// x~ = Dg^-1 (b_s - A_d' nu),  C = R_d^-1 + A_d Dg^-1 A_d'  (b_s: the
+// right-hand side without the dense rows), with C (r x r, r dense rows)
+// inverted once per factorisation.  A solve is then two sparse products over
+// the dense rows and one dense r x r product.
+// ---------------------------------------------------------------------------
+// Most dense rows of the form: C^-1 holds r^2 values per QP and a
+// factorisation costs about r^3 + r nnz(A_d) multiply-adds.
+constexpr int kDrMaxRows = 512;
+
+struct DrPlan {
+  int r = 0;
+  std::vector<int> rows;   // ascending rows of A with two or more entries
+};
+
+// 0 on success; 1 when P has an off-diagonal entry or there are more than rmax
+// dense rows (the form does not apply); 2 on inconsistent structure.
+inline int dr_plan_build(int n, int m, const int* Pp, const int* Pi, const int* Ap, const int* Ai, int rmax,
+                         DrPlan& pl) {
+  pl = DrPlan();
+  if (n <= 0 || m < 0) return 2;
+  for (int j = 0; j < n; j++)
+    for (int e = Pp[j]; e < Pp[j + 1]; e++) {
+      if (Pi[e] < 0 || Pi[e] > j) return 2;
+      if (Pi[e] != j) return 1;
+    }
+  std::vector<int> len(m, 0);
+  for (int j = 0; j < n; j++)
+    for (int e = Ap[j]; e < Ap[j + 1]; e++) {
+      if (Ai[e] < 0 || Ai[e] >= m) return 2;
+      len[Ai[e]]++;
+    }
+  for (int r = 0; r < m; r++)
+    if (len[r] >= 2) pl.rows.push_back(r);
+  pl.r = (int)pl.rows.size();
+  if (pl.r == 0 || pl.r > rmax) return 1;
+  return 0;
+}
+
+// Elements of the on-chip workspace: the factorisation's (a scatter vector of
+// n; C itself is formed in global memory), or the iteration's (right-hand
+// side and its second vector, x~ (n), w = rho z - y (m), then the (hi, lo)
+// pairs of t and nu, r each).
+GB_KKT_HD inline long long dr_ws_elems(int n, int m, int r) {
+  const long long f = kkt_pad4(n);
+  const long long v = kkt_pad4(2LL * n) + kkt_pad4(n) + kkt_pad4(m) + kkt_pad4(4LL * r);
+  return kkt_pad4(f > v ? f : v);
+}
+// Bytes: the elements, then on-chip copies of the dense-row list (r ints) and
+// of the row -> dense-row map (m ints).
+GB_KKT_HD inline long long dr_ws_bytes(int n, int m, int r, int elem) {
+  return dr_ws_elems(n, m, r) * elem + 4LL * (r + m);
+}
+
 }  // namespace gb

@@ -455,7 +455,7 @@ struct Solver {
   // and with cg_precond = 2 the inverted blocks of the block-Jacobi one
   template <typename G>
   __device__ void update_precond(G& g) {
-    if (pr.kkt.nb > 0) { direct_factor(g); return; }
+    if (kkt_direct(pr.kkt)) { direct_factor(g); return; }
     // local copies: hot loops keep the pointers in registers instead of
     // re-reading them through `this` after every store
     const DevProblem<T> pr = this->pr;
@@ -491,11 +491,76 @@ struct Solver {
   template <typename G>
   __device__ void direct_factor(G& g) {
     if constexpr (std::is_same<G, BlockGroup>::value) {
-      const bool ok = kkt_factor<T>(pr.kkt, pr.P, pr.A, pr.At, s.rho_is_vec ? pr.rho_vec : nullptr, (T)sc->rho,
-                                    (T)s.sigma, pr.kws);
+      const T* rv = s.rho_is_vec ? pr.rho_vec : nullptr;
+      const bool ok = pr.kkt.dr > 0
+                          ? dr_factor<T>(pr.kkt, pr.n, pr.P, pr.A, pr.At, rv, (T)sc->rho, (T)s.sigma, pr.kws)
+                          : kkt_factor<T>(pr.kkt, pr.P, pr.A, pr.At, rv, (T)sc->rho, (T)s.sigma, pr.kws);
       if (threadIdx.x == 0) sc->kkt_fail = ok ? 0 : 1;
       __syncthreads();
     }
+  }
+
+  // Diagonal-plus-dense-rows solve (gb_kkt_plan.h), in the saddle-point form
+  // of the builtin's KKT system restricted to the dense rows: with b_s the
+  // right-hand side without the dense rows' terms (kc on entry),
+  //   nu = C^-1 (A_d Dg^-1 b_s - (z_d - R_d^-1 y_d)),   x~ = Dg^-1 (b_s - A_d' nu),
+  // which equals K^-1 (b_s + A_d'(R_d z_d - y_d)) without forming that
+  // right-hand side: its rho-weighted dense-row terms would cancel in x~ and
+  // cost FP32 most of its digits.  The three products accumulate in
+  // double-float (FP32 build) and carry t and nu as (hi, lo) pairs, since a
+  // dense row sums many entries whose total nearly cancels.  kc becomes
+  // Dg^-1 b_s; x~ goes to kxs; tv: 4 r elements of on-chip scratch.  One warp
+  // per dense row for A_d u and C^-1 t, one warp per variable for A_d' nu
+  // (fixed lane order).
+  template <typename G>
+  __device__ void dr_solve(G& g, int n, T* kc, T* kxs, T* tv) {
+    const KktView<T>& kv = pr.kkt;
+    const bool vec = s.rho_is_vec;
+    const double rinv_s = sc->rho_inv;
+    const int r = kv.dr;
+    T* th = tv;
+    T* tl = tv + r;
+    T* nh = tv + 2 * r;
+    T* nl = tv + 3 * r;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for_n(g, n, [&](int i) { kc[i] = kc[i] * kv.Dginv[i]; });
+    __syncthreads();
+    for (int a = warp; a < r; a += nw) {
+      const int ra = kv.drows[a];
+      Acc<T> acc;
+      for (int e = pr.A.rowptr[ra] + lane; e < pr.A.rowptr[ra + 1]; e += 32) acc.add_prod(pr.A.val[e], kc[pr.A.col[e]]);
+      warp_accT(acc);
+      if (lane == 0) {
+        const double ri = vec ? (double)pr.rho_inv_vec[ra] : rinv_s;
+        const double t = acc.value() - ((double)pr.z[ra] - ri * (double)pr.y[ra]);
+        th[a] = (T)t;
+        tl[a] = (T)(t - (double)th[a]);
+      }
+    }
+    __syncthreads();
+    for (int a = warp; a < r; a += nw) {
+      const T* row = kv.Cinv + (size_t)a * r;
+      Acc<T> acc;
+      for (int b = lane; b < r; b += 32) { acc.add_prod(row[b], th[b]); acc.add_prod(row[b], tl[b]); }
+      warp_accT(acc);
+      if (lane == 0) {
+        const double v = acc.value();
+        nh[a] = (T)v;
+        nl[a] = (T)(v - (double)nh[a]);
+      }
+    }
+    __syncthreads();
+    const Rng rg = span_n(g, n);
+    for (int i = rg.lo + warp; i < rg.hi; i += nw) {
+      Acc<T> acc;
+      for (int e = pr.At.rowptr[i] + lane; e < pr.At.rowptr[i + 1]; e += 32) {
+        const int d = kv.didx[pr.At.col[e]];
+        if (d >= 0) { acc.add_prod(pr.At.val[e], nh[d]); acc.add_prod(pr.At.val[e], nl[d]); }
+      }
+      warp_accT(acc);
+      if (lane == 0) kxs[i] = (T)((double)kc[i] - (double)kv.Dginv[i] * acc.value());
+    }
+    __syncthreads();
   }
 
   template <typename G>
@@ -534,7 +599,7 @@ struct Solver {
     }
     __syncthreads();
     if (!prepare_data(g, false)) return false;
-    if (threadIdx.x == 0 && pr.kkt.nb > 0 && sc->kkt_fail) sc->status = ST_NON_CVX;
+    if (threadIdx.x == 0 && kkt_direct(pr.kkt) && sc->kkt_fail) sc->status = ST_NON_CVX;
     cold_start(g);
     return g.sync();
   }
@@ -555,7 +620,7 @@ struct Solver {
     const T rho_s = (T)sc->rho, rinv_s = (T)sc->rho_inv;
     T* __restrict__ x = pr.x; T* __restrict__ z = pr.z; T* __restrict__ y = pr.y;
     T* __restrict__ xp = pr.xp;
-    const bool direct = pr.kkt.nb > 0;
+    const bool direct = kkt_direct(pr.kkt);
     T* const kc = pr.kws;            // direct: permuted right-hand side
     const bool prof = s.profile && threadIdx.x == 0;
     long long pt = prof ? clock64() : 0;
@@ -575,9 +640,12 @@ struct Solver {
       __syncthreads();
     }
     if (prof) { const long long t = clock64(); sc->prof[0] += (unsigned long long)(t - pt); pt = t; }
+    // the dense-row form leaves its dense rows out of the right-hand side (they
+    // enter its solve through z - rho^-1 y, dr_solve)
+    const int* const ddx = pr.kkt.dr > 0 ? pr.kkt.didx : nullptr;
     rows_rng(g, span_n(g, n), pr.At,
       [&](int j) {
-        if (direct) return kw[j];
+        if (direct) return (ddx && ddx[j] >= 0) ? T(0) : kw[j];
         const T rj = vec ? pr.rho_vec[j] : rho_s;
         const T ij = vec ? pr.rho_inv_vec[j] : rinv_s;
         return rj * (z[j] - ij * y[j]);
@@ -585,7 +653,7 @@ struct Solver {
       [&](int i, T v) {
         const T b1 = sig * x[i] - pr.q[i];
         const T rr = b1 + v;
-        if (direct) kc[kip[i]] = rr;
+        if (direct) kc[kip ? kip[i] : i] = rr;
         else pr.rhs[i] = rr;
         mx0[0] = tmax(mx0[0], (T)fabs(rr));
       });
@@ -633,6 +701,9 @@ struct Solver {
     if (direct) {
       // x~ = K^-1 rhs (gb_direct.cuh), kept on chip (kxs)
       if constexpr (std::is_same<G, BlockGroup>::value) {
+       if (pr.kkt.dr > 0) {
+        dr_solve(g, n, kc, kxs, kw + kkt_pad4(m));
+       } else {
         const bool piped = pr.kkt.ring >= 2 && pr.kpipe;
         if (piped)
           kkt_solve_pipe<T>(pr.kkt, pr.kpipe, kc, kc + n, kc + kkt_pad4(2LL * n),
@@ -644,6 +715,7 @@ struct Solver {
           sc->prof[12] += 1;
           if (piped) { sc->prof[13] += 1; if (pr.kpipe->err) sc->prof[14] += 1; }
         }
+       }
       }
     } else {
       const int pcg_it = pcg_core(g, eps, sig, rho_s);
@@ -1244,7 +1316,7 @@ struct Solver {
     }
     if (it_lo <= 1 && !s.warm_starting) { cold_start(g); }
     if (!g.sync()) return false;
-    if (pr.kkt.nb > 0 && sc->kkt_fail) {
+    if (kkt_direct(pr.kkt) && sc->kkt_fail) {
       // the factorisation for this rho failed: K is not positive definite
       if (threadIdx.x == 0) { sc->status = ST_NON_CVX; sc->obj_val = NAN; sc->iter = it_lo > 1 ? it_lo - 1 : 0; }
       __syncthreads();
@@ -1302,7 +1374,7 @@ struct Solver {
         if (s.rho_is_vec) { refresh_rho_vec(g); if (!g.sync()) return false; }
         update_precond(g);
         if (!g.sync()) return false;
-        if (pr.kkt.nb > 0 && sc->kkt_fail) {
+        if (kkt_direct(pr.kkt) && sc->kkt_fail) {
           if (threadIdx.x == 0) { sc->status = ST_NON_CVX; sc->obj_val = NAN; s_flags[0] = 3; }
           __syncthreads();
           stopped = true;

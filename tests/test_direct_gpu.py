@@ -166,11 +166,67 @@ def test_direct_nonconvex_status():
     b.cleanup()
 
 
-def test_direct_rejects_dense_coupling():
-    # a budget row over every asset makes one block of all of them
+def test_direct_rejects_dense_coupling_with_dense_p():
+    # a dense P couples every variable: no block ordering within the limit, and
+    # the dense-row form needs a diagonal P
     b = Batch(load("f32"))
-    rc = b.setup([pb.portfolio(4, n=400)], linsys_solver=DIRECT_SOLVER, **WORKLOAD)
+    rc = b.setup([pb.random_qp(4, n=200, m=400)], linsys_solver=DIRECT_SOLVER, **WORKLOAD)
     assert rc == 3   # OSQP_LINSYS_SOLVER_INIT_ERROR
+
+
+def test_direct_dense_rows_portfolio_matches_builtin(oracle_lib, capsys):
+    """Factor-model portfolios (FP64 build): the budget row and the factor rows
+    couple every asset, so the direct solver takes the diagonal-plus-dense-rows
+    form (K = Dg + A_d' R_d A_d, inverse capacitance matrix) and follows the
+    builtin's trajectory; then two steps of drifting mean returns (new q)
+    through the batch update, the oracle updated the same way."""
+    prec = "f64"
+    probs = [pb.portfolio(seed=30 + i, n=n) for i, n in enumerate((100, 160, 250, 400, 640, 900))]
+    b = Batch(load(prec))
+    assert b.setup(probs, linsys_solver=DIRECT_SOLVER, **WORKLOAD) == 0
+    assert b.solve() == 0
+    sol = b.solution()
+    xs = b.split(sol["x"], "n")
+    orc = []
+    res = []
+    for d in probs:
+        o, r = oracle_solve(oracle_lib, d)
+        orc.append(o)
+        res.append(r)
+    with capsys.disabled():
+        bad, err, ratio = compare(res, probs, sol, xs, f"{prec} portfolio", print)
+    assert not bad, bad
+    check_bars(prec, probs, res, sol, xs, err, ratio, oracle_lib)
+    rg = np.random.default_rng(31)
+    for step in range(2):
+        qs = [(d[1] * (1.0 + 0.02 * rg.standard_normal(d[1].size))) for d in probs]
+        assert b.update(q=np.concatenate(qs)) == 0
+        assert b.solve() == 0
+        sol = b.solution()
+        xs = b.split(sol["x"], "n")
+        res = []
+        for o, q2 in zip(orc, qs):
+            o.update(q=q2)
+            res.append(o.solve())
+        cur = [(d[0], q2, d[2], d[3], d[4]) for d, q2 in zip(probs, qs)]
+        with capsys.disabled():
+            bad, err, ratio = compare(res, cur, sol, xs, f"{prec} portfolio step {step}", print)
+        assert not bad, bad
+        check_bars(prec, cur, res, sol, xs, err, ratio, oracle_lib)
+    rows, cinv, dginv = b.dense_rows(5)
+    P, q, A, l, u = probs[5]
+    assert np.array_equal(rows, np.flatnonzero(np.diff(A.tocsr().indptr) >= 2))
+    assert cinv.shape == (len(rows), len(rows)) and np.allclose(cinv, cinv.T, rtol=0, atol=0)
+    assert np.all(dginv > 0)
+    b.cleanup()
+
+
+def test_direct_dense_rows_fp32_keeps_pcg():
+    """The FP32 build does not take the dense-row form (its FP32 iterates left
+    such QPs far from the builtin's iteration counts): set-up is refused and
+    the PCG serves them."""
+    b = Batch(load("f32"))
+    assert b.setup([pb.portfolio(seed=33, n=400)], linsys_solver=DIRECT_SOLVER, **WORKLOAD) == 3
 
 
 @pytest.mark.parametrize("prec", ["f32", "f64"])
