@@ -273,6 +273,49 @@ __device__ __forceinline__ bool stage_problem(DevProblem<TT>& pr, const Spans& s
   return true;
 }
 
+// Shared-memory staging for a direct solve (one CTA), in the room after the
+// direct solver's workspace: the CSR row pointers of A, A' and P (every
+// sparse-product row starts with them), then the QP's vectors in the order
+// an ADMM iteration touches them -- z, y, the rho vector and its inverse, l,
+// u, dy (m), x, q, dx (n) -- while they fit, then CSR entries of A', A and P
+// while room remains.  The vectors are copied in (dir > 0) and back (dir <
+// 0); row pointers and entries are copied in.  The layout is a pure function
+// of the sizes, so the copy-back call recomputes it.
+template <typename TT>
+__device__ __forceinline__ bool stage_direct(DevProblem<TT>& pr, bool rho_vec, unsigned char* base, int cap, int dir,
+                                             bool matrices) {
+  Stager<TT> sg{base, cap, 0, dir};
+  const int n = pr.n, m = pr.m;
+  DevProblem<TT> q = pr;
+  const int* growA = pr.A.rowptr;
+  const int* growAt = pr.At.rowptr;
+  const int* growP = pr.P.rowptr;
+  if (m) q.A.rowptr = sg.rows(pr.A.rowptr, 0, m);
+  q.At.rowptr = sg.rows(pr.At.rowptr, 0, n);
+  q.P.rowptr = sg.rows(pr.P.rowptr, 0, n);
+  if (m) {
+    q.z = sg.span(pr.z, 0, m, true);
+    q.y = sg.span(pr.y, 0, m, true);
+    if (rho_vec) {
+      q.rho_vec = sg.span(pr.rho_vec, 0, m, true);
+      q.rho_inv_vec = sg.span(pr.rho_inv_vec, 0, m, true);
+    }
+    q.l = sg.span(pr.l, 0, m, true);
+    q.u = sg.span(pr.u, 0, m, true);
+    q.dy = sg.span(pr.dy, 0, m, true);
+  }
+  q.x = sg.span(pr.x, 0, n, true);
+  q.q = sg.span(pr.q, 0, n, true);
+  q.dx = sg.span(pr.dx, 0, n, true);
+  if (matrices) {
+    sg.entries(q.At, growAt, 0, n);
+    if (m) sg.entries(q.A, growA, 0, m);
+    sg.entries(q.P, growP, 0, n);
+  }
+  pr = q;
+  return true;
+}
+
 // Contiguous slices of a QP's rows for rank r of a c-CTA cluster, balanced by
 // estimated work: a row costs its entries plus 4 x (lanes per row), the
 // entries a sub-warp could have processed in the row's fixed per-row work.
@@ -321,15 +364,24 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   // direct KKT solve: the dynamic shared memory is the factorisation's and the
   // block solve's workspace (the QP's data stay in HBM / L2)
   const bool direct = kkt_direct(pv.kkt);
+  int dstage = 0;   // direct solve: offset of the staged QP data in dsm (0: none)
   if (direct) {
     pv.kws = (TT*)dsm;
     pv.kpipe = kpipe;
+    long long wsb;
     if (pv.kkt.dr > 0) {
       dr_on_chip(pv.kkt, (int*)(dsm + dr_ws_elems(pv.n, pv.m, pv.kkt.dr) * sizeof(TT)), pv.m);
+      wsb = dr_ws_bytes(pv.n, pv.m, pv.kkt.dr, (int)sizeof(TT));
     } else {
       if (!kpipe) pv.kkt.ring = 0;
       kkt_plan_on_chip(pv.kkt, (int*)(dsm + kkt_ws_elems(pv.n, pv.m, pv.kkt.bmax, pv.kkt.segmax, pv.kkt.ring) * sizeof(TT)),
                        pv.n);
+      wsb = kkt_ws_bytes(pv.n, pv.m, pv.kkt.bmax, pv.kkt.nb, pv.kkt.segmax, pv.kkt.ring, (int)sizeof(TT));
+    }
+    const int off = (int)((wsb + 15) & ~15LL);
+    if (mode == kModeSolve && stage_mat >= 0 && off + 1024 < dsm_bytes) {
+      dstage = off;
+      staged = stage_direct(pv, s.rho_is_vec != 0, dsm + off, dsm_bytes - off, 1, stage_mat != 0);
     }
     __syncthreads();
   }
@@ -375,7 +427,8 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
   g.sync();
   if (staged) {
     DevProblem<TT> pb = B.problem(k);
-    stage_problem(pb, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, -1, stage_mat != 0, stage_mat == 2);
+    if (dstage) stage_direct(pb, s.rho_is_vec != 0, dsm + dstage, dsm_bytes - dstage, -1, stage_mat != 0);
+    else stage_problem(pb, g.sp, s.rho_is_vec != 0, dsm, dsm_bytes, -1, stage_mat != 0, stage_mat == 2);
     g.sync();   // peers may still read this CTA's copies until here
   }
   if constexpr (std::is_same<G, ClusterGroup>::value) {
@@ -902,6 +955,9 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     if (ao && cudaMemcpy(hAi.data(), Ai, sizeof(OSQPInt) * ao, cudaMemcpyDefault) != cudaSuccess) { delete b; return OSQP_DATA_VALIDATION_ERROR; }
     plans.resize(count);
     drplans.resize(count);
+    // ring slots of the block solve's copy pipeline: deeper rings measured no
+    // faster, and the room they leave holds the QP's vectors on chip
+    const int ring_max = std::max(2, std::min(kKktRingMax, env_int("OSQP_GB300_KKT_RING_SLOTS", 4)));
     std::vector<int> prc(count, 0), ring(count, 0);
     const int nthr = std::max(1, std::min((int)std::thread::hardware_concurrency(), std::min(count, 64)));
     std::vector<std::thread> pool;
@@ -928,7 +984,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
           }
           if (!prc[k]) {
             // ring slots of the solve's bulk-copy pipeline: as many as fit (at least 2), else none
-            int R = kKktRingMax;
+            int R = ring_max;
             while (R >= 2 && kkt_ws_bytes(I.n, I.m, plans[k].bmax, plans[k].nb, plans[k].segmax, R, (int)sizeof(T)) > b->dsm) R--;
             if (R < 2) R = 0;
             if (kkt_ws_bytes(I.n, I.m, plans[k].bmax, plans[k].nb, plans[k].segmax, R, (int)sizeof(T)) > b->dsm) prc[k] = 3;
