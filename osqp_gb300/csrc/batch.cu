@@ -645,9 +645,20 @@ using namespace gbb;
 
 typedef void (*BatchKernel)(BatchArrays<T>, DevSettings, BatchLaunch);
 
-// The CTA form's kernel for a CTA size (512 threads x 2 per SM, or 1024 x 1).
-static void cta_form(int threads, BatchKernel* fn, int* nt, int* minb) {
+static int env_int(const char* name, int dflt);
+
+// The CTA form's kernel: 1024 threads x 1 per SM, 512 x 2, or 512 x 1 (128
+// registers per thread), from OSQP_GB300_BATCH_THREADS and
+// OSQP_GB300_BATCH_CTAS_PER_SM.  Defaults measured on 4096 batched MPC QPs
+// (one box, alternating): the PCG runs 1024 x 1 (512 x 2: -7 %); the direct
+// solver runs 512 x 1 (against 1024 x 1: +4.7 % FP64, +6.7 % FP32; its block
+// solve uses a few warps, and the sparse products of the FP64 build are bound
+// by the FP64 pipe rather than by the number of warps).
+static void cta_form(bool direct, BatchKernel* fn, int* nt, int* minb) {
+  const int threads = env_int("OSQP_GB300_BATCH_THREADS", direct ? 512 : 1024);
+  const int per_sm = env_int("OSQP_GB300_BATCH_CTAS_PER_SM", direct ? 1 : 2);
   if (threads >= 1024) { *fn = k_batch<T, 1024, 1>; *nt = 1024; *minb = 1; }
+  else if (per_sm == 1) { *fn = k_batch<T, kBatchThreads, 1>; *nt = kBatchThreads; *minb = 1; }
   else { *fn = k_batch<T, kBatchThreads, 2>; *nt = kBatchThreads; *minb = 2; }
 }
 // The cluster form's kernel for a CTA size (one CTA per SM).
@@ -948,7 +959,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
   if (b->direct) {
     // the factorisation and the block solve work in the CTA's shared memory
     int minb0 = 1;
-    cta_form(env_int("OSQP_GB300_BATCH_THREADS", 1024), &b->kfn, &b->threads, &minb0);
+    cta_form(true, &b->kfn, &b->threads, &minb0);
     b->dsm = configure_dsm(b->kfn, b->threads, minb0, b->device, cap_kib0 < 0 ? -1L : 1024L * cap_kib0);
     const int blim = kkt_bmax_limit(b->threads, b->dsm, (int)sizeof(T));
     std::vector<OSQPInt> hAi(ao > 0 ? ao : 1);
@@ -1211,7 +1222,7 @@ extern "C" OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, con
     else b->grid = std::max(1, std::min(count, nclusters));   // grid counted in clusters
   }
   int minb = 2;
-  cta_form(env_int("OSQP_GB300_BATCH_THREADS", 1024), &b->kfn, &b->threads, &minb);
+  cta_form(b->direct != 0, &b->kfn, &b->threads, &minb);
   b->dsm = configure_dsm(b->kfn, b->threads, minb, b->device, cap);
   if (b->cluster == 0) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->kfn, b->threads, (size_t)b->dsm);

@@ -11,7 +11,9 @@
 //   so a rerun reproduces every bit and all CTAs of a group obtain identical
 //   scalars, which lets each CTA keep its own copy of the solver's scalar state.
 // * CSR row kernels with 1..32 lanes per row (sub-warp per row), several rows
-//   in flight per lane group.
+//   in flight per lane group; for the FP64 build, dense batches of 32 rows per
+//   warp whose follow-up work runs one row per lane, and maxima and bound
+//   tests on the integer pipe (FP64 instructions are slow on GB300).
 #pragma once
 
 #include <cooperative_groups.h>
@@ -138,6 +140,89 @@ template <typename T>
 __device__ __forceinline__ void warp_accT(Acc<T>& a) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) a.shfl_merge(o);
+}
+
+// ---------------------------------------------------------------------------
+// Maxima and bound tests on the integer pipe.
+//
+// GB300 issues an FP64 warp instruction in about 65-77 cycles of its SM
+// sub-partition, whatever the number of active lanes, and the FP64 max and
+// compare instructions (DMNMX, DSETP) go down that pipe too.  Maxima of |v|
+// are therefore kept as bit patterns (nonnegative IEEE numbers order as
+// their patterns) and reduced with integer compares; signed maxima use the
+// usual order-preserving map of the pattern.  A NaN is ignored, as the
+// reference's infinity norm ignores it (its test |v_i| > max is false for
+// NaN).  Comparisons of a value with a positive threshold use the signed
+// integer view of the pattern: for p > 0, v > p iff bits(v) > bits(p) and
+// v < p iff bits(v) < bits(p), for every v that is not NaN.
+// ---------------------------------------------------------------------------
+template <typename T> struct FKey;
+template <> struct FKey<double> {
+  typedef unsigned long long U;
+  typedef long long I;
+  static constexpr U kAbs = 0x7fffffffffffffffull, kInf = 0x7ff0000000000000ull, kSign = 0x8000000000000000ull;
+  static __device__ __forceinline__ I bits(double v) { return __double_as_longlong(v); }
+  static __device__ __forceinline__ U absk(double v) {
+    const U b = (U)bits(v) & kAbs;
+    return b > kInf ? 0ull : b;
+  }
+  // order key of a signed value; NaN maps below every number
+  static __device__ __forceinline__ U key(double v) {
+    const U b = (U)bits(v);
+    if ((b & kAbs) > kInf) return 0ull;
+    return (b & kSign) ? ~b : (b | kSign);
+  }
+  static __device__ __forceinline__ U key_neg(double v) { return key(__longlong_as_double((I)((U)bits(v) ^ kSign))); }
+  static __device__ __forceinline__ double from_absk(U k) { return __longlong_as_double((I)k); }
+  static __device__ __forceinline__ double from_key(U k) { return __longlong_as_double((I)((k & kSign) ? (k & kAbs) : ~k)); }
+  // v > p / v < p for p > 0 given pb = bits(p); the same for -v
+  static __device__ __forceinline__ bool gt(double v, I pb) { return bits(v) > pb; }
+  static __device__ __forceinline__ bool lt(double v, I pb) { return bits(v) < pb; }
+  static __device__ __forceinline__ bool neg_gt(double v, I pb) { return (I)((U)bits(v) ^ kSign) > pb; }
+  static __device__ __forceinline__ bool neg_lt(double v, I pb) { return (I)((U)bits(v) ^ kSign) < pb; }
+  // |v| < p for p > 0
+  static __device__ __forceinline__ bool abs_lt(double v, I pb) { return (I)((U)bits(v) & kAbs) < pb; }
+  // max(v, 0) and min(v, 0) as `v > 0 ? v : 0` and `v < 0 ? v : 0`
+  static __device__ __forceinline__ double pos(double v) { return bits(v) > 0 ? v : 0.0; }
+  static __device__ __forceinline__ double neg(double v) { return (bits(v) < 0 && ((U)bits(v) << 1) != 0) ? v : 0.0; }
+  // thresholds: bits of p for `v > p` and for `v < p` (p is a double)
+  static __device__ __forceinline__ I thr_gt(double p) { return bits(p); }
+  static __device__ __forceinline__ I thr_lt(double p) { return bits(p); }
+};
+template <> struct FKey<float> {
+  typedef unsigned U;
+  typedef int I;
+  static constexpr U kAbs = 0x7fffffffu, kInf = 0x7f800000u, kSign = 0x80000000u;
+  static __device__ __forceinline__ I bits(float v) { return __float_as_int(v); }
+  static __device__ __forceinline__ U absk(float v) {
+    const U b = (U)bits(v) & kAbs;
+    return b > kInf ? 0u : b;
+  }
+  static __device__ __forceinline__ U key(float v) {
+    const U b = (U)bits(v);
+    if ((b & kAbs) > kInf) return 0u;
+    return (b & kSign) ? ~b : (b | kSign);
+  }
+  static __device__ __forceinline__ U key_neg(float v) { return key(__int_as_float((I)((U)bits(v) ^ kSign))); }
+  static __device__ __forceinline__ float from_absk(U k) { return __int_as_float((I)k); }
+  static __device__ __forceinline__ float from_key(U k) { return __int_as_float((I)((k & kSign) ? (k & kAbs) : ~k)); }
+  static __device__ __forceinline__ bool gt(float v, I pb) { return bits(v) > pb; }
+  static __device__ __forceinline__ bool lt(float v, I pb) { return bits(v) < pb; }
+  static __device__ __forceinline__ bool neg_gt(float v, I pb) { return (I)((U)bits(v) ^ kSign) > pb; }
+  static __device__ __forceinline__ bool neg_lt(float v, I pb) { return (I)((U)bits(v) ^ kSign) < pb; }
+  static __device__ __forceinline__ bool abs_lt(float v, I pb) { return (I)((U)bits(v) & kAbs) < pb; }
+  static __device__ __forceinline__ float pos(float v) { return bits(v) > 0 ? v : 0.f; }
+  static __device__ __forceinline__ float neg(float v) { return (bits(v) < 0 && ((U)bits(v) << 1) != 0) ? v : 0.f; }
+  // a float v exceeds the double p iff it exceeds the largest float <= p, and
+  // is below p iff it is below the smallest float >= p
+  static __device__ __forceinline__ I thr_gt(double p) { return bits(__double2float_rd(p)); }
+  static __device__ __forceinline__ I thr_lt(double p) { return bits(__double2float_ru(p)); }
+};
+template <typename U> __device__ __forceinline__ U umaxk(U a, U b) { return a > b ? a : b; }
+template <typename U> __device__ __forceinline__ U warp_umax(U v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = umaxk(v, (U)__shfl_xor_sync(0xffffffffu, v, o));
+  return v;
 }
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -308,13 +393,19 @@ struct BlockGroup {
   // FP64 results in rs / rm.  fn(rsum, rmax), if given, runs once (thread 0)
   // on the results before they are published, for scalar follow-up math
   // whose outputs go to shared memory (bd / bf / bi).
-  template <typename T, int NS, int NM, typename FN = NoFn>
+  // reduce_w: the same with maxima already reduced across each warp (every
+  // lane holds its warp's maximum)
+  template <typename T, int NS, int NM>
+  __device__ void reduce_w(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM]) {
+    reduce<T, NS, NM, NoFn, true>(s, m, rs, rm, NoFn());
+  }
+  template <typename T, int NS, int NM, typename FN = NoFn, bool WD = false>
   __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM], FN fn = FN()) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) sh->wsum[w][i] = acc_pack<T>(s[i]); }
 #pragma unroll
-    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
+    for (int i = 0; i < NM; i++) { T v = WD ? m[i] : warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
     __syncthreads();
     if constexpr (NS + NM <= 4) {
       // small reductions: warp 0 finishes every slot, lane 0 runs fn
@@ -380,7 +471,13 @@ struct ClusterGroup {
   // per-CTA partials into every CTA's `recv` (DSMEM stores), then after one
   // cluster barrier every CTA merges the ranks' partials in rank order from
   // its own shared memory, so all CTAs obtain identical values.
-  template <typename T, int NS, int NM, typename FN = NoFn>
+  // reduce_w: the same with maxima already reduced across each warp (every
+  // lane holds its warp's maximum)
+  template <typename T, int NS, int NM>
+  __device__ void reduce_w(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM]) {
+    reduce<T, NS, NM, NoFn, true>(s, m, rs, rm, NoFn());
+  }
+  template <typename T, int NS, int NM, typename FN = NoFn, bool WD = false>
   __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM], FN fn = FN()) {
     namespace cgr = cooperative_groups;
     cgr::cluster_group cl = cgr::this_cluster();
@@ -389,7 +486,7 @@ struct ClusterGroup {
 #pragma unroll
     for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) sh->wsum[w][i] = acc_pack<T>(s[i]); }
 #pragma unroll
-    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
+    for (int i = 0; i < NM; i++) { T v = WD ? m[i] : warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
     __syncthreads();
     const int par = sh->parity;
     if (w == 0) {
@@ -484,13 +581,19 @@ struct GridGroup {
   }
   __device__ bool ok() const { return sh->flag == 0; }
 
-  template <typename T, int NS, int NM, typename FN = NoFn>
+  // reduce_w: the same with maxima already reduced across each warp (every
+  // lane holds its warp's maximum)
+  template <typename T, int NS, int NM>
+  __device__ void reduce_w(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM]) {
+    reduce<T, NS, NM, NoFn, true>(s, m, rs, rm, NoFn());
+  }
+  template <typename T, int NS, int NM, typename FN = NoFn, bool WD = false>
   __device__ void reduce(Acc<T> (&s)[NS], T (&m)[NM], double (&rs)[NS], double (&rm)[NM], FN fn = FN()) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < NS; i++) { warp_accT(s[i]); if (lane == 0) sh->wsum[w][i] = acc_pack<T>(s[i]); }
 #pragma unroll
-    for (int i = 0; i < NM; i++) { T v = warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
+    for (int i = 0; i < NM; i++) { T v = WD ? m[i] : warp_maxT(m[i]); if (lane == 0) sh->wmax[w][i] = max_pack<T>(v); }
     __syncthreads();
     const int nw = blockDim.x >> 5, nb = gridDim.x;
     const int par = sh->parity;
@@ -717,7 +820,7 @@ __device__ __forceinline__ void for_m(G& g, int m, FN fn) { for_rng(g, span_m(g,
 // same order.
 constexpr int kRowsInFlight = 2;
 
-template <int L, int NR, typename T, typename XF>
+template <int L, int NR, int U = kRowUnroll, typename T, typename XF>
 __device__ __forceinline__ void lane_rows_dot(const int* const (&col)[NR], const T* const (&val)[NR],
                                               const int (&b)[NR], const int (&e)[NR], int sl, XF xf,
                                               T (&acc)[NR]) {
@@ -726,27 +829,27 @@ __device__ __forceinline__ void lane_rows_dot(const int* const (&col)[NR], const
 #pragma unroll
   for (int r = 0; r < NR; r++) { k[r] = b[r] + sl; more |= k[r] < e[r]; }
   while (more) {
-    int c[NR][kRowUnroll];
-    T v[NR][kRowUnroll];
+    int c[NR][U];
+    T v[NR][U];
 #pragma unroll
     for (int r = 0; r < NR; r++)
 #pragma unroll
-      for (int u = 0; u < kRowUnroll; u++) {
+      for (int u = 0; u < U; u++) {
         const int kk = k[r] + u * L;
         c[r][u] = kk < e[r] ? col[r][kk] : -1;
         v[r][u] = kk < e[r] ? val[r][kk] : T(0);
       }
-    T x[NR][kRowUnroll];
+    T x[NR][U];
 #pragma unroll
     for (int r = 0; r < NR; r++)
 #pragma unroll
-      for (int u = 0; u < kRowUnroll; u++) x[r][u] = c[r][u] >= 0 ? xf(c[r][u]) : T(0);
+      for (int u = 0; u < U; u++) x[r][u] = c[r][u] >= 0 ? xf(c[r][u]) : T(0);
     more = false;
 #pragma unroll
     for (int r = 0; r < NR; r++) {
 #pragma unroll
-      for (int u = 0; u < kRowUnroll; u++) acc[r] += v[r][u] * x[r][u];
-      k[r] += kRowUnroll * L;
+      for (int u = 0; u < U; u++) acc[r] += v[r][u] * x[r][u];
+      k[r] += U * L;
       more |= k[r] < e[r];
     }
   }
@@ -824,6 +927,219 @@ __device__ __forceinline__ void rows_rng2(G& g, Rng rg, const CSR<T>& M, XF1 a, 
     case 8:  rows_rng2_L<8>(g, rg, M, a, b, fn); break;
     case 16: rows_rng2_L<16>(g, rg, M, a, b, fn); break;
     default: rows_rng2_L<32>(g, rg, M, a, b, fn); break;
+  }
+}
+
+// ---- dense row batches: one row per lane for the follow-up work ----
+//
+// Rows [rg.lo, rg.hi) of M in batches of 32 consecutive rows per warp.  Each
+// sub-warp of L lanes sums one row's entries exactly as rows_rng_L does (lane
+// sl takes entries b+sl, b+sl+L, ... in order, then subwarp_sum), NR rows in
+// flight per lane; the batch's 32 sums then move by shuffles so that lane t
+// holds row base + t, and fn(row, value) runs on every lane that has a row.
+// Element-wise follow-up work so issues one warp instruction per 32 rows
+// instead of one per 32 / L rows, which matters for FP64 work on GB300 (an
+// FP64 warp instruction costs the same whatever the number of active lanes).
+
+// Two products of NR rows per lane (shared index and value loads), entries
+// summed per lane in ascending order as lane_row_dot2.
+template <int L, int NR, int U = 1, typename T, typename XF1, typename XF2>
+__device__ __forceinline__ void lane_rows_dot2(const int* const (&col)[NR], const T* const (&val)[NR],
+                                               const int (&b)[NR], const int (&e)[NR], int sl, XF1 xf1, XF2 xf2,
+                                               T (&a1)[NR], T (&a2)[NR]) {
+  int k[NR];
+  bool more = false;
+#pragma unroll
+  for (int r = 0; r < NR; r++) { k[r] = b[r] + sl; more |= k[r] < e[r]; }
+  while (more) {
+    int c[NR][U];
+    T v[NR][U];
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int kk = k[r] + u * L;
+        c[r][u] = kk < e[r] ? col[r][kk] : -1;
+        v[r][u] = kk < e[r] ? val[r][kk] : T(0);
+      }
+    more = false;
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const T x1 = c[r][u] >= 0 ? xf1(c[r][u]) : T(0);
+        const T x2 = c[r][u] >= 0 ? xf2(c[r][u]) : T(0);
+        a1[r] += v[r][u] * x1;
+        a2[r] += v[r][u] * x2;
+      }
+      k[r] += U * L;
+      more |= k[r] < e[r];
+    }
+  }
+}
+
+// Entries per lane loaded before any is used in the dense row batches: one
+// product (rows_dense) takes four, two products (rows_dense2 / _pair) one.
+// Measured on 4096 batched MPC QPs, FP64 direct solver (one box): four in
+// both forms gave the single products -11 % / -16 % cycles and the
+// termination's pairs +13 %.
+constexpr int kDenseUnroll = 4;
+constexpr int kDenseUnroll2 = 1;
+
+template <int L>
+struct DenseRows {
+  static constexpr int RPW = 32 / L;            // rows per sub-iteration
+  static constexpr int NR = L < 2 ? L : 2;      // rows in flight per lane
+  // shuffle source lane and sub-iteration of this lane's row
+  static __device__ __forceinline__ int src(int lane) { return (lane % RPW) * L; }
+  static __device__ __forceinline__ int mine(int lane) { return lane / RPW; }
+};
+
+template <int L, typename T, typename G, typename XF, typename FN>
+__device__ __forceinline__ void rows_dense_L(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
+  typedef DenseRows<L> D;
+  constexpr int NR = D::NR;
+  const int lane = threadIdx.x & 31, sub = lane / L, sl = lane % L;
+  const int src = D::src(lane), mine = D::mine(lane);
+  for (int base = rg.lo + g.w0() * 32; base < rg.hi; base += g.ws() * 32) {
+    T res = T(0);
+#pragma unroll 1
+    for (int u0 = 0; u0 < L; u0 += NR) {
+      const int* col[NR];
+      const T* val[NR];
+      int b[NR], e[NR];
+      T acc[NR];
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const int row = base + (u0 + r) * D::RPW + sub;
+        row_ptrs(M, row, row < rg.hi, col[r], val[r], b[r], e[r]);
+        acc[r] = T(0);
+      }
+      lane_rows_dot<L, NR, kDenseUnroll>(col, val, b, e, sl, xf, acc);
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const T a = __shfl_sync(0xffffffffu, subwarp_sum<L>(acc[r]), src);
+        if (mine == u0 + r) res = a;
+      }
+    }
+    if (base + lane < rg.hi) fn(base + lane, res);
+  }
+}
+template <typename T, typename G, typename XF, typename FN>
+__device__ __forceinline__ void rows_dense(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
+  switch (M.lanes) {
+    case 1:  rows_dense_L<1>(g, rg, M, xf, fn); break;
+    case 2:  rows_dense_L<2>(g, rg, M, xf, fn); break;
+    case 4:  rows_dense_L<4>(g, rg, M, xf, fn); break;
+    case 8:  rows_dense_L<8>(g, rg, M, xf, fn); break;
+    case 16: rows_dense_L<16>(g, rg, M, xf, fn); break;
+    default: rows_dense_L<32>(g, rg, M, xf, fn); break;
+  }
+}
+
+template <int L, typename T, typename G, typename XF1, typename XF2, typename FN>
+__device__ __forceinline__ void rows_dense2_L(G& g, Rng rg, const CSR<T>& M, XF1 xf1, XF2 xf2, FN fn) {
+  typedef DenseRows<L> D;
+  constexpr int NR = D::NR;
+  const int lane = threadIdx.x & 31, sub = lane / L, sl = lane % L;
+  const int src = D::src(lane), mine = D::mine(lane);
+  for (int base = rg.lo + g.w0() * 32; base < rg.hi; base += g.ws() * 32) {
+    T r1 = T(0), r2 = T(0);
+#pragma unroll 1
+    for (int u0 = 0; u0 < L; u0 += NR) {
+      const int* col[NR];
+      const T* val[NR];
+      int b[NR], e[NR];
+      T a1[NR], a2[NR];
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const int row = base + (u0 + r) * D::RPW + sub;
+        row_ptrs(M, row, row < rg.hi, col[r], val[r], b[r], e[r]);
+        a1[r] = T(0);
+        a2[r] = T(0);
+      }
+      lane_rows_dot2<L, NR, kDenseUnroll2>(col, val, b, e, sl, xf1, xf2, a1, a2);
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const T v1 = __shfl_sync(0xffffffffu, subwarp_sum<L>(a1[r]), src);
+        const T v2 = __shfl_sync(0xffffffffu, subwarp_sum<L>(a2[r]), src);
+        if (mine == u0 + r) { r1 = v1; r2 = v2; }
+      }
+    }
+    if (base + lane < rg.hi) fn(base + lane, r1, r2);
+  }
+}
+template <typename T, typename G, typename XF1, typename XF2, typename FN>
+__device__ __forceinline__ void rows_dense2(G& g, Rng rg, const CSR<T>& M, XF1 a, XF2 b, FN fn) {
+  switch (M.lanes) {
+    case 1:  rows_dense2_L<1>(g, rg, M, a, b, fn); break;
+    case 2:  rows_dense2_L<2>(g, rg, M, a, b, fn); break;
+    case 4:  rows_dense2_L<4>(g, rg, M, a, b, fn); break;
+    case 8:  rows_dense2_L<8>(g, rg, M, a, b, fn); break;
+    case 16: rows_dense2_L<16>(g, rg, M, a, b, fn); break;
+    default: rows_dense2_L<32>(g, rg, M, a, b, fn); break;
+  }
+}
+
+// Dense row batches for the FP64 build on a CTA or a cluster, where the
+// follow-up work is FP64 instructions; sub-warp rows (rows_rng) for the FP32
+// build (its follow-up work is cheap on the FP32 pipe) and for the grid form
+// (one large QP), where sub-warp rows spread more evenly over the grid's
+// warps.  fn(row, value) alike in both.
+template <typename T, typename G>
+constexpr bool kDenseRows = std::is_same<T, double>::value && !std::is_same<G, GridGroup>::value;
+template <typename T, typename G, typename XF, typename FN>
+__device__ __forceinline__ void rows_auto(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
+  if constexpr (kDenseRows<T, G>) rows_dense(g, rg, M, xf, fn);
+  else rows_rng(g, rg, M, xf, fn);
+}
+template <typename T, typename G, typename XF1, typename XF2, typename FN>
+__device__ __forceinline__ void rows_auto2(G& g, Rng rg, const CSR<T>& M, XF1 a, XF2 b, FN fn) {
+  if constexpr (kDenseRows<T, G>) rows_dense2(g, rg, M, a, b, fn);
+  else rows_rng2(g, rg, M, a, b, fn);
+}
+
+// Two matrices with the same rows (P and A'), two products each:
+// fn(row, M1 x1, M1 x2, M2 y1, M2 y2) with one row per lane; L lanes per row
+// for both matrices.
+template <int L, typename T, typename G, typename XP1, typename XP2, typename XA1, typename XA2, typename FN>
+__device__ __forceinline__ void rows_dense_pair_L(G& g, Rng rg, const CSR<T>& M1, const CSR<T>& M2, XP1 xp1, XP2 xp2,
+                                                  XA1 xa1, XA2 xa2, FN fn) {
+  typedef DenseRows<L> D;
+  constexpr int NR = D::NR;
+  const int lane = threadIdx.x & 31, sub = lane / L, sl = lane % L;
+  const int src = D::src(lane), mine = D::mine(lane);
+  for (int base = rg.lo + g.w0() * 32; base < rg.hi; base += g.ws() * 32) {
+    T r1 = T(0), r2 = T(0), r3 = T(0), r4 = T(0);
+#pragma unroll 1
+    for (int u0 = 0; u0 < L; u0 += NR) {
+      const int* col[NR];
+      const T* val[NR];
+      int b[NR], e[NR];
+      T a1[NR], a2[NR], a3[NR], a4[NR];
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const int row = base + (u0 + r) * D::RPW + sub;
+        row_ptrs(M1, row, row < rg.hi, col[r], val[r], b[r], e[r]);
+        a1[r] = a2[r] = a3[r] = a4[r] = T(0);
+      }
+      lane_rows_dot2<L, NR, kDenseUnroll2>(col, val, b, e, sl, xp1, xp2, a1, a2);
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const int row = base + (u0 + r) * D::RPW + sub;
+        row_ptrs(M2, row, row < rg.hi, col[r], val[r], b[r], e[r]);
+      }
+      lane_rows_dot2<L, NR, kDenseUnroll2>(col, val, b, e, sl, xa1, xa2, a3, a4);
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const T v1 = __shfl_sync(0xffffffffu, subwarp_sum<L>(a1[r]), src);
+        const T v2 = __shfl_sync(0xffffffffu, subwarp_sum<L>(a2[r]), src);
+        const T v3 = __shfl_sync(0xffffffffu, subwarp_sum<L>(a3[r]), src);
+        const T v4 = __shfl_sync(0xffffffffu, subwarp_sum<L>(a4[r]), src);
+        if (mine == u0 + r) { r1 = v1; r2 = v2; r3 = v3; r4 = v4; }
+      }
+    }
+    if (base + lane < rg.hi) fn(base + lane, r1, r2, r3, r4);
   }
 }
 

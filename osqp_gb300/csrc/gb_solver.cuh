@@ -643,7 +643,7 @@ struct Solver {
     // the dense-row form leaves its dense rows out of the right-hand side (they
     // enter its solve through z - rho^-1 y, dr_solve)
     const int* const ddx = pr.kkt.dr > 0 ? pr.kkt.didx : nullptr;
-    rows_rng(g, span_n(g, n), pr.At,
+    rows_auto(g, span_n(g, n), pr.At,
       [&](int j) {
         if (direct) return (ddx && ddx[j] >= 0) ? T(0) : kw[j];
         const T rj = vec ? pr.rho_vec[j] : rho_s;
@@ -653,27 +653,43 @@ struct Solver {
       [&](int i, T v) {
         const T b1 = sig * x[i] - pr.q[i];
         const T rr = b1 + v;
-        if (direct) kc[kip ? kip[i] : i] = rr;
-        else pr.rhs[i] = rr;
-        mx0[0] = tmax(mx0[0], (T)fabs(rr));
+        if (direct) {
+          kc[kip ? kip[i] : i] = rr;
+        } else {
+          pr.rhs[i] = rr;
+          mx0[0] = tmax(mx0[0], (T)fabs(rr));   // the PCG's tolerance only
+        }
       });
     if (m > 0 && !direct) {
       rows_rng(g, span_m(g, m), pr.A, [&](int c) { return xp[c]; },
         [&](int j, T v) { g.put(pr.t, j, (vec ? pr.rho_vec[j] : rho_s) * v); });
     }
     if (prof) { const long long t = clock64(); sc->prof[9] += (unsigned long long)(t - pt); pt = t; }
-    // time / cancellation ride on this reduction so every CTA sees the same values
-    if (g.tid() == 0) {
-      mx0[1] = (T)((double)(global_ns() - sc->t_start) * 1e-9);
-      const int cw = *((volatile int*)&pr.st->cancel);
-      mx0[2] = (s.cancel_gen > 0 && cw == s.cancel_gen) ? T(1) : T(0);
+    double rhs_norm = 0.0, elapsed = 0.0;
+    int cancel = 0;
+    if (direct && std::is_same<G, BlockGroup>::value) {
+      // one CTA: thread 0, the only reader of the time and the cancel word,
+      // reads them itself; the barrier completes the right-hand side
+      if (threadIdx.x == 0) {
+        elapsed = (double)(T)((double)(global_ns() - sc->t_start) * 1e-9);
+        const int cw = *((volatile int*)&pr.st->cancel);
+        cancel = s.cancel_gen > 0 && cw == s.cancel_gen;
+      }
+      __syncthreads();
+    } else {
+      // time / cancellation ride on this reduction so every CTA sees the same values
+      if (g.tid() == 0) {
+        mx0[1] = (T)((double)(global_ns() - sc->t_start) * 1e-9);
+        const int cw = *((volatile int*)&pr.st->cancel);
+        mx0[2] = (s.cancel_gen > 0 && cw == s.cancel_gen) ? T(1) : T(0);
+      }
+      double rs0[1], rm0[3];
+      g.reduce(sm0, mx0, rs0, rm0);
+      if (!g.ok()) return false;
+      rhs_norm = rm0[0];
+      elapsed = rm0[1];
+      cancel = rm0[2] > 0.0;
     }
-    double rs0[1], rm0[3];
-    g.reduce(sm0, mx0, rs0, rm0);
-    if (!g.ok()) return false;
-    const double rhs_norm = rm0[0];
-    const double elapsed = rm0[1];
-    const int cancel = rm0[2] > 0.0;
     if (prof) { const long long t = clock64(); sc->prof[0] += (unsigned long long)(t - pt); pt = t; }
 
     // PCG tolerance (cuda_pcg_interface.cu:32-64), computed once per CTA
@@ -737,7 +753,7 @@ struct Solver {
     });
     if (prof) { const long long t = clock64(); sc->prof[2] += (unsigned long long)(t - pt); pt = t; }
     if (m > 0) {
-      rows_rng(g, span_m(g, m), pr.A, [&](int c) { return direct ? kxs[c] : xp[c]; }, [&](int j, T zt) {
+      rows_auto(g, span_m(g, m), pr.A, [&](int c) { return direct ? kxs[c] : xp[c]; }, [&](int j, T zt) {
         const T ri = vec ? pr.rho_inv_vec[j] : rinv_s;
         const T rr = vec ? pr.rho_vec[j] : rho_s;
         const T zo = z[j];
@@ -1087,121 +1103,150 @@ struct Solver {
     const bool uns = unscaled_term();
     T* x = pr.x; T* z = pr.z; T* y = pr.y;
 
+    // Maxima are integer keys (FKey): on GB300 the FP64 max / compare
+    // instructions would cost a slow FP64 warp instruction each.  The bound
+    // tests compare bit patterns with the thresholds (l and u are never NaN).
+    typedef FKey<T> K;
+    typedef typename K::U U;
+    typedef typename K::I I;
+    const I inf_gt = K::thr_gt(infval), inf_lt = K::thr_lt(infval), dz_lt = K::thr_lt(s.zero_deadzone);
+
     // Phase T1 over the rows of A: Ax, A dx and the m-length terms.
     // mx: 0 |Ax-z|  1 |Einv(Ax-z)|  2 |z|  3 |Ax|  4 |Einv z|  5 |Einv Ax|
-    //     6 |dy_proj|  7 |E dy_proj|  8 recession-cone violation of (Einv) A dx
+    //     6 |dy_proj| (|E dy_proj| for unscaled termination)
+    //     7 recession-cone violation of (Einv) A dx
     // sm: 0 support function  1 u'max(dy,0) + l'min(dy,0)
     Acc<T> sm[2];
-    T mx[9];
+    U km[8];
 #pragma unroll
-    for (int k = 0; k < 9; k++) mx[k] = (k == 8) ? T(-INFINITY) : T(0);
+    for (int k = 0; k < 7; k++) km[k] = 0;
+    km[7] = K::key(T(-INFINITY));
     if (m > 0) {
-      rows_rng2(g, span_m(g, m), pr.A, [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; },
+      rows_auto2(g, span_m(g, m), pr.A, [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; },
         [&](int j, T ax, T adx) {
           const T l = pr.l[j], u = pr.u[j];
           const T ei = pr.Einv[j];
           const T zj = z[j];
           const T pres = ax - zj;
-          mx[0] = tmax(mx[0], (T)fabs(pres));
-          mx[1] = tmax(mx[1], (T)fabs(ei * pres));
-          mx[2] = tmax(mx[2], (T)fabs(zj));
-          mx[3] = tmax(mx[3], (T)fabs(ax));
-          mx[4] = tmax(mx[4], (T)fabs(ei * zj));
-          mx[5] = tmax(mx[5], (T)fabs(ei * ax));
+          km[0] = umaxk(km[0], K::absk(pres));
+          km[1] = umaxk(km[1], K::absk(ei * pres));
+          km[2] = umaxk(km[2], K::absk(zj));
+          km[3] = umaxk(km[3], K::absk(ax));
+          km[4] = umaxk(km[4], K::absk(ei * zj));
+          km[5] = umaxk(km[5], K::absk(ei * ax));
+          const bool u_inf = K::gt(u, inf_gt);       // u > infval
+          const bool l_inf = K::neg_gt(l, inf_gt);   // l < -infval
           // support function of [l,u] at y (auxil.c:254-266)
           T yp = y[j];
-          if ((double)u > infval) yp = ((double)l < -infval) ? T(0) : tmin(yp, T(0));
-          else if ((double)l < -infval) yp = tmax(yp, T(0));
-          if (fabs((double)yp) < s.zero_deadzone) yp = T(0);
-          sm[0].add_prod(u, tmax(yp, T(0)));
-          sm[0].add_prod(l, tmin(yp, T(0)));
+          if (u_inf) yp = l_inf ? T(0) : K::neg(yp);
+          else if (l_inf) yp = K::pos(yp);
+          if (K::abs_lt(yp, dz_lt)) yp = T(0);
+          sm[0].add_prod(u, K::pos(yp));
+          sm[0].add_prod(l, K::neg(yp));
           // project dy onto the polar recession cone (in place) (auxil.c:476-480)
           T dp = pr.dy[j];
-          if ((double)u > infval) dp = ((double)l < -infval) ? T(0) : tmin(dp, T(0));
-          else if ((double)l < -infval) dp = tmax(dp, T(0));
+          if (u_inf) dp = l_inf ? T(0) : K::neg(dp);
+          else if (l_inf) dp = K::pos(dp);
           pr.dy[j] = dp;
-          mx[6] = tmax(mx[6], (T)fabs(dp));
-          mx[7] = tmax(mx[7], (T)fabs(pr.E[j] * dp));
-          sm[1].add_prod(u, tmax(dp, T(0)));
-          sm[1].add_prod(l, tmin(dp, T(0)));
+          km[6] = umaxk(km[6], K::absk(uns ? pr.E[j] * dp : dp));
+          sm[1].add_prod(u, K::pos(dp));
+          sm[1].add_prod(l, K::neg(dp));
           // recession cone test of A dx (vector.c:704-727): violation if
           // (u finite and v > tol) or (l finite and v < -tol)
           const T v = uns ? adx * ei : adx;
-          T viol = T(-INFINITY);
-          if ((double)u < infval) viol = tmax(viol, v);
-          if ((double)l > -infval) viol = tmax(viol, -v);
-          mx[8] = tmax(mx[8], viol);
+          if (K::lt(u, inf_lt)) km[7] = umaxk(km[7], K::key(v));          // u < infval
+          if (K::neg_lt(l, inf_lt)) km[7] = umaxk(km[7], K::key_neg(v));  // l > -infval
         });
     }
-    double smr[2], mxr[9];
-    g.reduce(sm, mx, smr, mxr);
+    T mx[8];
+#pragma unroll
+    for (int k = 0; k < 7; k++) mx[k] = K::from_absk(warp_umax(km[k]));
+    mx[7] = K::from_key(warp_umax(km[7]));
+    double smr[2], mxr[8];
+    g.reduce_w(sm, mx, smr, mxr);
     if (!g.ok()) return false;
 
     // Phase T2 over the rows of P / A': Px, P dx, A'y, A'dy and the n-length terms.
     // mx: 0 |q+Px+A'y|  1 |Dinv(q+Px+A'y)|  2 |q|  3 |A'y|  4 |Px|  5 |Dinv q|
-    //     6 |Dinv A'y|  7 |Dinv Px|  8 |dx|  9 |D dx|  10 |P dx|  11 |Dinv P dx|
-    //     12 |A'dy|  13 |Dinv A'dy|
+    //     6 |Dinv A'y|  7 |Dinv Px|  8 |dx|  9 |P dx|  10 |A'dy| (8-10 with
+    //     D, Dinv, Dinv for unscaled termination)
     // sm: 0 x'Px  1 q'x  2 q'dx
     Acc<T> s2[3];
-    T m2[14];
+    U k2[11];
 #pragma unroll
-    for (int k = 0; k < 14; k++) m2[k] = T(0);
+    for (int k = 0; k < 11; k++) k2[k] = 0;
     {
-      const int L = kktL;
-      auto body = [&](auto Lc) {
-        constexpr int LL = decltype(Lc)::value;
-        const int lane = threadIdx.x & 31;
-        const int sub = lane / LL, sl = lane % LL;
-        constexpr int RPW = 32 / LL;
-        const Rng rg = span_n(g, n);
-        const int ws = g.ws();
-        for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += ws * RPW) {
-          const int i = base + sub;
-          T px = T(0), pdx = T(0), aty = T(0), atdy = T(0);
-          if (i < rg.hi) {
-            lane_row_dot2<LL>(pr.P.col, pr.P.val, pr.P.rowptr[i], pr.P.rowptr[i + 1], sl,
-                              [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; }, px, pdx);
-            lane_row_dot2<LL>(pr.At.col, pr.At.val, pr.At.rowptr[i], pr.At.rowptr[i + 1], sl,
-                              [&](int c) { return y[c]; }, [&](int c) { return pr.dy[c]; }, aty, atdy);
-          }
-          px = subwarp_sum<LL>(px); pdx = subwarp_sum<LL>(pdx);
-          aty = subwarp_sum<LL>(aty); atdy = subwarp_sum<LL>(atdy);
-          if (i < rg.hi && sl == 0) {
-            const T q = pr.q[i];
-            const T di = pr.Dinv[i];
-            const T dr = (m > 0) ? (q + px) + aty : q + px;
-            m2[0] = tmax(m2[0], (T)fabs(dr));
-            m2[1] = tmax(m2[1], (T)fabs(di * dr));
-            m2[2] = tmax(m2[2], (T)fabs(q));
-            m2[3] = tmax(m2[3], (T)fabs(aty));
-            m2[4] = tmax(m2[4], (T)fabs(px));
-            m2[5] = tmax(m2[5], (T)fabs(di * q));
-            m2[6] = tmax(m2[6], (T)fabs(di * aty));
-            m2[7] = tmax(m2[7], (T)fabs(di * px));
-            const T dxi = pr.dx[i];
-            m2[8] = tmax(m2[8], (T)fabs(dxi));
-            m2[9] = tmax(m2[9], (T)fabs(pr.D[i] * dxi));
-            m2[10] = tmax(m2[10], (T)fabs(pdx));
-            m2[11] = tmax(m2[11], (T)fabs(pdx * di));
-            m2[12] = tmax(m2[12], (T)fabs(atdy));
-            m2[13] = tmax(m2[13], (T)fabs(atdy * di));
-            s2[0].add_prod(px, x[i]);
-            s2[1].add_prod(q, x[i]);
-            s2[2].add_prod(q, dxi);
-          }
-        }
+      auto fn = [&](int i, T px, T pdx, T aty, T atdy) {
+        const T q = pr.q[i];
+        const T di = pr.Dinv[i];
+        const T dr = (m > 0) ? (q + px) + aty : q + px;
+        k2[0] = umaxk(k2[0], K::absk(dr));
+        k2[1] = umaxk(k2[1], K::absk(di * dr));
+        k2[2] = umaxk(k2[2], K::absk(q));
+        k2[3] = umaxk(k2[3], K::absk(aty));
+        k2[4] = umaxk(k2[4], K::absk(px));
+        k2[5] = umaxk(k2[5], K::absk(di * q));
+        k2[6] = umaxk(k2[6], K::absk(di * aty));
+        k2[7] = umaxk(k2[7], K::absk(di * px));
+        const T dxi = pr.dx[i];
+        k2[8] = umaxk(k2[8], K::absk(uns ? pr.D[i] * dxi : dxi));
+        k2[9] = umaxk(k2[9], K::absk(uns ? pdx * di : pdx));
+        k2[10] = umaxk(k2[10], K::absk(uns ? atdy * di : atdy));
+        s2[0].add_prod(px, x[i]);
+        s2[1].add_prod(q, x[i]);
+        s2[2].add_prod(q, dxi);
       };
-      switch (L) {
-        case 1:  body(std::integral_constant<int, 1>{}); break;
-        case 2:  body(std::integral_constant<int, 2>{}); break;
-        case 4:  body(std::integral_constant<int, 4>{}); break;
-        case 8:  body(std::integral_constant<int, 8>{}); break;
-        case 16: body(std::integral_constant<int, 16>{}); break;
-        default: body(std::integral_constant<int, 32>{}); break;
+      auto xp1 = [&](int c) { return x[c]; };
+      auto xp2 = [&](int c) { return pr.dx[c]; };
+      auto xa1 = [&](int c) { return y[c]; };
+      auto xa2 = [&](int c) { return pr.dy[c]; };
+      const Rng rg = span_n(g, n);
+      const int L = kktL;
+      if constexpr (std::is_same<G, GridGroup>::value || !std::is_same<T, double>::value) {
+        // one large QP: sub-warp rows keep every warp of the grid busy; FP32:
+        // the sub-warp epilogue is cheap on the FP32 pipe
+        auto body = [&](auto Lc) {
+          constexpr int LL = decltype(Lc)::value;
+          const int lane = threadIdx.x & 31;
+          const int sub = lane / LL, sl = lane % LL;
+          constexpr int RPW = 32 / LL;
+          const int ws = g.ws();
+          for (int base = rg.lo + g.w0() * RPW; base < rg.hi; base += ws * RPW) {
+            const int i = base + sub;
+            T px = T(0), pdx = T(0), aty = T(0), atdy = T(0);
+            if (i < rg.hi) {
+              lane_row_dot2<LL>(pr.P.col, pr.P.val, pr.P.rowptr[i], pr.P.rowptr[i + 1], sl, xp1, xp2, px, pdx);
+              lane_row_dot2<LL>(pr.At.col, pr.At.val, pr.At.rowptr[i], pr.At.rowptr[i + 1], sl, xa1, xa2, aty, atdy);
+            }
+            px = subwarp_sum<LL>(px); pdx = subwarp_sum<LL>(pdx);
+            aty = subwarp_sum<LL>(aty); atdy = subwarp_sum<LL>(atdy);
+            if (i < rg.hi && sl == 0) fn(i, px, pdx, aty, atdy);
+          }
+        };
+        switch (L) {
+          case 1:  body(std::integral_constant<int, 1>{}); break;
+          case 2:  body(std::integral_constant<int, 2>{}); break;
+          case 4:  body(std::integral_constant<int, 4>{}); break;
+          case 8:  body(std::integral_constant<int, 8>{}); break;
+          case 16: body(std::integral_constant<int, 16>{}); break;
+          default: body(std::integral_constant<int, 32>{}); break;
+        }
+      } else {
+        switch (L) {
+          case 1:  rows_dense_pair_L<1>(g, rg, pr.P, pr.At, xp1, xp2, xa1, xa2, fn); break;
+          case 2:  rows_dense_pair_L<2>(g, rg, pr.P, pr.At, xp1, xp2, xa1, xa2, fn); break;
+          case 4:  rows_dense_pair_L<4>(g, rg, pr.P, pr.At, xp1, xp2, xa1, xa2, fn); break;
+          case 8:  rows_dense_pair_L<8>(g, rg, pr.P, pr.At, xp1, xp2, xa1, xa2, fn); break;
+          case 16: rows_dense_pair_L<16>(g, rg, pr.P, pr.At, xp1, xp2, xa1, xa2, fn); break;
+          default: rows_dense_pair_L<32>(g, rg, pr.P, pr.At, xp1, xp2, xa1, xa2, fn); break;
+        }
       }
     }
-    double s2r[3], m2r[14];
-    g.reduce(s2, m2, s2r, m2r);
+    T m2[11];
+#pragma unroll
+    for (int k = 0; k < 11; k++) m2[k] = K::from_absk(warp_umax(k2[k]));
+    double s2r[3], m2r[11];
+    g.reduce_w(s2, m2, s2r, m2r);
     if (!g.ok()) return false;
 
     if (threadIdx.x == 0) {
@@ -1232,13 +1277,13 @@ struct Solver {
       c->nq_s = m2r[2]; c->nAty_s = m2r[3]; c->nPx_s = m2r[4];
       c->nq_u = m2r[5]; c->nAty_u = m2r[6]; c->nPx_u = m2r[7];
       // infeasibility quantities
-      c->dy_norm = uns ? mxr[7] : mxr[6];
+      c->dy_norm = mxr[6];
       c->dy_lhs = smr[1];
-      c->atdy_norm = uns ? m2r[13] : m2r[12];
-      c->dx_norm = uns ? m2r[9] : m2r[8];
+      c->atdy_norm = m2r[10];
+      c->dx_norm = m2r[8];
       c->dx_q = s2r[2];
-      c->pdx_norm = uns ? m2r[11] : m2r[10];
-      c->recc_max = mxr[8];
+      c->pdx_norm = m2r[9];
+      c->recc_max = mxr[7];
     }
     __syncthreads();
     return true;
