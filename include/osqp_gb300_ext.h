@@ -153,8 +153,9 @@ OSQPInt osqp_gb300_batch_structure(OSQPBatch* batch, OSQPInt k, OSQPInt which, O
  * updates; the issuing of the direct solve's bulk copies (cycles[0..11],
  * thread 0's view, the last by the issuing thread), then counts of direct
  * solves: all, through the bulk-copy ring, and of those the ones that read
- * the factor from global memory after a failed wait (cycles[12..14];
- * cycles[15] unused); zeros unless the
+ * the factor from global memory after a failed wait (cycles[12..14]), and
+ * the cycles thread 0 spends in the block products of the sweeps
+ * (cycles[15]); zeros unless the
  * batch was set up with OSQP_GB300_PROFILE=1 in the environment).  No
  * reference counterpart (the reference's profiler_level times host phases). */
 OSQPInt osqp_gb300_batch_phase_cycles(OSQPBatch* batch, double* cycles);

@@ -470,7 +470,7 @@ class Batch:
         self.L.lib.osqp_gb300_batch_phase_cycles(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return dict(zip(["rhs", "linsys", "updates", "termination", "refactor", "linsys_wait", "linsys_barrier",
                          "linsys_forward", "linsys_backward", "rhs_spmv", "updates_spmv", "linsys_issue",
-                         "direct_solves", "direct_solves_ring", "direct_solves_global", "unused"],
+                         "direct_solves", "direct_solves_ring", "direct_solves_global", "linsys_dot"],
                         out.tolist()))
 
     def dense_rows(self, k: int):

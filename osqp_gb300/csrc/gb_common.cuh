@@ -855,7 +855,10 @@ __device__ __forceinline__ void lane_rows_dot(const int* const (&col)[NR], const
   }
 }
 
-// Row r's entry pointers: the on-chip copy below M.srow, else HBM.
+// Row r's entry pointers: the on-chip copy below M.srow, else HBM.  (The
+// row loops take their CSR descriptor by value: a descriptor inside a larger
+// struct in memory would be reloaded after every store through the generic
+// vector pointers, which could alias it.)
 template <typename T>
 __device__ __forceinline__ void row_ptrs(const CSR<T>& M, int r, bool valid, const int*& col, const T*& val,
                                          int& b, int& e) {
@@ -867,7 +870,7 @@ __device__ __forceinline__ void row_ptrs(const CSR<T>& M, int r, bool valid, con
 }
 
 template <int L, typename T, typename G, typename XF, typename FN>
-__device__ __forceinline__ void rows_rng_L(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
+__device__ __forceinline__ void rows_rng_L(G& g, Rng rg, const CSR<T> M, XF xf, FN fn) {
   constexpr int NR = kRowsInFlight;
   const int lane = threadIdx.x & 31;
   const int sub = lane / L, sl = lane % L;
@@ -904,7 +907,7 @@ __device__ __forceinline__ void rows_rng(G& g, Rng rg, const CSR<T>& M, XF xf, F
   }
 }
 template <int L, typename T, typename G, typename XF1, typename XF2, typename FN>
-__device__ __forceinline__ void rows_rng2_L(G& g, Rng rg, const CSR<T>& M, XF1 xf1, XF2 xf2, FN fn) {
+__device__ __forceinline__ void rows_rng2_L(G& g, Rng rg, const CSR<T> M, XF1 xf1, XF2 xf2, FN fn) {
   const int lane = threadIdx.x & 31;
   const int sub = lane / L, sl = lane % L;
   constexpr int RPW = 32 / L;
@@ -996,7 +999,7 @@ struct DenseRows {
 };
 
 template <int L, typename T, typename G, typename XF, typename FN>
-__device__ __forceinline__ void rows_dense_L(G& g, Rng rg, const CSR<T>& M, XF xf, FN fn) {
+__device__ __forceinline__ void rows_dense_L(G& g, Rng rg, const CSR<T> M, XF xf, FN fn) {
   typedef DenseRows<L> D;
   constexpr int NR = D::NR;
   const int lane = threadIdx.x & 31, sub = lane / L, sl = lane % L;
@@ -1038,7 +1041,7 @@ __device__ __forceinline__ void rows_dense(G& g, Rng rg, const CSR<T>& M, XF xf,
 }
 
 template <int L, typename T, typename G, typename XF1, typename XF2, typename FN>
-__device__ __forceinline__ void rows_dense2_L(G& g, Rng rg, const CSR<T>& M, XF1 xf1, XF2 xf2, FN fn) {
+__device__ __forceinline__ void rows_dense2_L(G& g, Rng rg, const CSR<T> M, XF1 xf1, XF2 xf2, FN fn) {
   typedef DenseRows<L> D;
   constexpr int NR = D::NR;
   const int lane = threadIdx.x & 31, sub = lane / L, sl = lane % L;
@@ -1103,7 +1106,7 @@ __device__ __forceinline__ void rows_auto2(G& g, Rng rg, const CSR<T>& M, XF1 a,
 // fn(row, M1 x1, M1 x2, M2 y1, M2 y2) with one row per lane; L lanes per row
 // for both matrices.
 template <int L, typename T, typename G, typename XP1, typename XP2, typename XA1, typename XA2, typename FN>
-__device__ __forceinline__ void rows_dense_pair_L(G& g, Rng rg, const CSR<T>& M1, const CSR<T>& M2, XP1 xp1, XP2 xp2,
+__device__ __forceinline__ void rows_dense_pair_L(G& g, Rng rg, const CSR<T> M1, const CSR<T> M2, XP1 xp1, XP2 xp2,
                                                   XA1 xa1, XA2 xa2, FN fn) {
   typedef DenseRows<L> D;
   constexpr int NR = D::NR;

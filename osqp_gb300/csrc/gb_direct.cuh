@@ -66,6 +66,114 @@ struct KktView {
 template <typename T>
 __host__ __device__ inline bool kkt_direct(const KktView<T>& kv) { return kv.nb > 0 || kv.dr > 0; }
 
+// ---------------------------------------------------------------------------
+// Double-float block solve of the FP64 build.
+//
+// GB300 runs FP64 at about 1/64 of the FP32 rate: an FP64 warp instruction
+// takes 65-77 cycles of its SM sub-partition, and a block step is a chain of
+// small dense products on a few warps.  The FP64 build therefore factors K in
+// FP64 but stores the factor as double-float pairs (a float hi and a float
+// lo with hi + lo = the FP64 entry to 48 significant bits), and runs the
+// block solve in double-float on the FP32 pipe: the two solve vectors are
+// (hi, lo) pairs, each product row is a compensated dot product (the exact
+// product of the high parts by FMA plus the cross terms, partial sums kept
+// error-free by TwoSum and their errors summed apart: the Dot2 scheme of
+// Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26 (2005)).  The right-hand side enters and the solution leaves in
+// FP64.  A factor sub-array of len entries keeps its bytes: the hi words of
+// all entries, then (after kkt_pad4(len) words) the lo words.
+// ---------------------------------------------------------------------------
+#ifndef GB_KKT_DF
+#define GB_KKT_DF 1
+#endif
+template <typename T>
+constexpr bool kKktDF = GB_KKT_DF && std::is_same<T, double>::value;
+
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF df_split(double v) {
+  const float h = __double2float_rn(v);
+  return DF{h, __double2float_rn(v - (double)h)};
+}
+__device__ __forceinline__ double df_join(DF a) { return (double)a.h + (double)a.l; }
+// (s, e) = a + b exactly (Knuth's TwoSum)
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// a - b, renormalised
+__device__ __forceinline__ DF df_sub(DF a, DF b) {
+  float s, e;
+  df_two_sum(a.h, -b.h, s, e);
+  e = __fadd_rn(e, __fsub_rn(a.l, b.l));
+  const float h = __fadd_rn(s, e);
+  return DF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+// Value type of one block-product row: T, or DF in the double-float solve.
+template <typename T>
+using kkt_val = typename std::conditional<kKktDF<T>, DF, T>::type;
+
+// Entry o of a factor sub-array of len entries starting at base.
+template <typename T>
+__device__ __forceinline__ void kkt_fstore(T* base, long long len, long long o, T v) {
+  if constexpr (kKktDF<T>) {
+    float* f = reinterpret_cast<float*>(base);
+    const DF s = df_split(v);
+    f[o] = s.h;
+    f[kkt_pad4(len) + o] = s.l;
+  } else {
+    base[o] = v;
+  }
+}
+
+// The solve's permuted n-vectors (c, d): T values, or in the double-float
+// solve the hi words of the n entries followed by their lo words (the same
+// bytes as n doubles).
+template <typename T>
+__device__ __forceinline__ void kkt_vput(T* v, int n, int i, T x) {
+  if constexpr (kKktDF<T>) {
+    float* f = reinterpret_cast<float*>(v);
+    const DF s = df_split(x);
+    f[i] = s.h;
+    f[n + i] = s.l;
+  } else {
+    v[i] = x;
+  }
+}
+template <typename T>
+__device__ __forceinline__ T kkt_vget(const T* v, int n, int i) {
+  if constexpr (kKktDF<T>) {
+    const float* f = reinterpret_cast<const float*>(v);
+    return df_join(DF{f[i], f[n + i]});
+  } else {
+    return v[i];
+  }
+}
+template <typename T>
+__device__ __forceinline__ void kkt_vset(T* v, int n, int i, kkt_val<T> a) {
+  if constexpr (kKktDF<T>) {
+    float* f = reinterpret_cast<float*>(v);
+    f[i] = a.h;
+    f[n + i] = a.l;
+  } else {
+    v[i] = a;
+  }
+}
+template <typename T>
+__device__ __forceinline__ void kkt_vsub(T* v, int n, int i, kkt_val<T> a) {
+  if constexpr (kKktDF<T>) {
+    float* f = reinterpret_cast<float*>(v);
+    const DF r = df_sub(DF{f[i], f[n + i]}, a);
+    f[i] = r.h;
+    f[n + i] = r.l;
+  } else {
+    v[i] -= a;
+  }
+}
+
 // Factor K = P + sigma I + A' R A (scaled data) into F.  ws: on-chip
 // workspace of kkt_factor_ws_elems(bmax) elements.  rho_vec == nullptr: the
 // scalar rho.  Returns false when a pivot is not positive (K not positive
@@ -188,8 +296,8 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
       T* GTg = kv.F + kv.bo[k];
       for (int o = tid; o < b * bp; o += nt) {
         const int j = o / b, i = o - j * b;
-        Gg[o] = G[i * bp + j];
-        GTg[o] = G[o];
+        kkt_fstore(Gg, (long long)b * bp, o, G[i * bp + j]);
+        kkt_fstore(GTg, (long long)b * bp, o, G[o]);
       }
       __syncthreads();
     }
@@ -219,7 +327,7 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
     }
     for (int o = tid; o < b * b; o += nt) {
       const T v = -src[o];
-      Sg[o] = v;
+      kkt_fstore(Sg, (long long)b * b, o, v);
       Sprev[o] = v;
     }
     __syncthreads();
@@ -234,21 +342,85 @@ __device__ __noinline__ bool kkt_factor(const KktView<T>& kv, const CSR<T>& P, c
 // whole number of warps.
 __host__ __device__ inline int kkt_half(int bmax) { return bmax <= 32 ? 32 : ((bmax + 31) & ~31); }
 
-// sum_j M[j rows + r] v[j]: row r of a column-major rows x cols block, by one
-// thread, in four interleaved partial sums (fixed order).
-template <typename T>
-__device__ __forceinline__ T kkt_col_dot(const T* __restrict__ M, const T* __restrict__ v, int rows, int cols,
-                                         int r) {
-  T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
-  int j = 0;
-  for (; j + 4 <= cols; j += 4) {
-    a0 += M[(size_t)j * rows + r] * v[j];
-    a1 += M[(size_t)(j + 1) * rows + r] * v[j + 1];
-    a2 += M[(size_t)(j + 2) * rows + r] * v[j + 2];
-    a3 += M[(size_t)(j + 3) * rows + r] * v[j + 3];
+// Lanes per block row in the solve (Q): each row's product is split over Q
+// consecutive lanes, so a step's chain of dependent multiply-adds is Q times
+// shorter and more of the CTA's warps work on it.  The widest of 4, 2, 1
+// whose group (two halves of kkt_group_half threads) leaves a warp for the
+// producer.  Measured per step on batched MPC (blocks of ~34): one lane per
+// row spent ~130 cycles per double-float term, latency rather than issue.
+__host__ __device__ inline int kkt_group_half(int bmax, int q) {
+  const int t = q * bmax;
+  return t <= 32 ? 32 : ((t + 31) & ~31);
+}
+__host__ __device__ inline int kkt_lanes(int bmax, int threads) {
+  for (int q = 4; q > 1; q >>= 1)
+    if (2 * kkt_group_half(bmax, q) + 32 <= threads) return q;
+  return 1;
+}
+
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s, e;
+  df_two_sum(a.h, b.h, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, e);
+  return DF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+// Row r of the column-major rows x cols block M times entries off.. of the
+// solve vector v (n entries), by the Q consecutive lanes q = 0..Q-1 of a lane
+// group: lane q takes columns q, q + Q, ... in two interleaved partial sums
+// (compensated in the double-float solve), then the group adds its partials
+// by xor shuffles, so every lane of the group gets the same value.  Every lane
+// of the warp calls it; a lane group without a row passes active = false.
+template <int Q, typename T>
+__device__ __forceinline__ kkt_val<T> kkt_dot_q(const T* M, const T* v, int n, int off, int rows, int cols, int r,
+                                               int q, bool active) {
+  const int ce = active ? cols : 0;
+  if constexpr (kKktDF<T>) {
+    const float* __restrict__ Mh = reinterpret_cast<const float*>(M);
+    const float* __restrict__ Ml = Mh + kkt_pad4((long long)rows * cols);
+    const float* __restrict__ vh = reinterpret_cast<const float*>(v) + off;
+    const float* __restrict__ vl = vh + n;
+    float s0 = 0.f, s1 = 0.f, c0 = 0.f, c1 = 0.f;
+    auto term = [&](int j, float& sa, float& ca) {
+      const size_t o = (size_t)j * rows + r;
+      const float mh = Mh[o], ml = Ml[o], xh = vh[j], xl = vl[j];
+      const float p = __fmul_rn(mh, xh);
+      const float e = __fmaf_rn(mh, xl, __fmaf_rn(ml, xh, __fmaf_rn(mh, xh, -p)));
+      float t, es;
+      df_two_sum(sa, p, t, es);
+      sa = t;
+      ca = __fadd_rn(ca, __fadd_rn(es, e));
+    };
+    int j = q;
+    for (; j + Q < ce; j += 2 * Q) {
+      term(j, s0, c0);
+      term(j + Q, s1, c1);
+    }
+    if (j < ce) term(j, s0, c0);
+    float S, es;
+    df_two_sum(s0, s1, S, es);
+    const float C = __fadd_rn(__fadd_rn(c0, c1), es);
+    const float h = __fadd_rn(S, C);
+    DF a{h, __fsub_rn(C, __fsub_rn(h, S))};
+#pragma unroll
+    for (int o = Q / 2; o > 0; o >>= 1)
+      a = df_add(a, DF{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)});
+    return a;
+  } else {
+    const T* __restrict__ x = v + off;
+    T a0 = T(0), a1 = T(0);
+    int j = q;
+    for (; j + Q < ce; j += 2 * Q) {
+      a0 += M[(size_t)j * rows + r] * x[j];
+      a1 += M[(size_t)(j + Q) * rows + r] * x[j + Q];
+    }
+    if (j < ce) a0 += M[(size_t)j * rows + r] * x[j];
+    T a = a0 + a1;
+#pragma unroll
+    for (int o = Q / 2; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    return a;
   }
-  for (; j < cols; j++) a0 += M[(size_t)j * rows + r] * v[j];
-  return (a0 + a1) + (a2 + a3);
 }
 
 // Barrier of the solve group only (named barrier 1; `threads` a multiple of 32).
@@ -350,29 +522,40 @@ __device__ __forceinline__ void kkt_arrive(unsigned long long* bar) {
 // j % ring.  The producer (the first thread after the group) issues copy j
 // once the group released copy j - ring; the group releases a copy after the
 // step that last reads it, so every copy of a solve is released by its end.
-// Needs blockDim.x >= 2 kkt_half(bmax) + 32.
+// Needs blockDim.x >= 2 kkt_half(bmax) + 32 (kkt_lanes picks the lanes per
+// row from the rest).
 template <typename T, typename XO>
 __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T* ring, XO xout,
-                               unsigned long long* prof = nullptr, unsigned long long* prof_issue = nullptr) {
+                               unsigned long long* prof = nullptr, unsigned long long* prof_issue = nullptr,
+                               unsigned long long* prof_dot = nullptr) {
+  // the view's fields as locals: kv lives in memory that the stores through
+  // the generic solve-vector pointers could alias, so every use would reload it
+  const int* const bs = kv.bs;
+  const int* const fo = kv.fo;
+  const int* const bo = kv.bo;
+  const int* const perm = kv.perm;
+  const T* const F = kv.F;
   // prof (thread 0 only, optional): cycles spent [0] waiting for segments, [1]
   // in group barriers, [2] in the forward sweep, [3] in the backward sweep
-  const int H = kkt_half(kv.bmax), GT = 2 * H;
+  const int QL = kkt_lanes(kv.bmax, blockDim.x);
+  const int H = kkt_group_half(kv.bmax, QL), GT = 2 * H;
   const int tid = threadIdx.x;
   const int nb = kv.nb, R = kv.ring, SM = kv.segmax;
+  const int n = bs[nb];
   const int total = 2 * nb - 1;
   // parity of the wait for copy j (full) and of the release of copy j (empty)
   auto fpar = [&](int j) { return (pp->fph[j % R] + (unsigned)(j / R)) & 1u; };
   auto epar = [&](int j) { return (pp->eph[j % R] + (unsigned)(j / R)) & 1u; };
   auto seg = [&](int j, long long& elems) -> const T* {
     if (j < nb) {
-      const long long b = kv.bs[j + 1] - kv.bs[j], bp = j ? kv.bs[j] - kv.bs[j - 1] : 0;
+      const long long b = bs[j + 1] - bs[j], bp = j ? bs[j] - bs[j - 1] : 0;
       elems = kkt_pad4(b * bp) + kkt_pad4(b * b);
-      return kv.F + kv.fo[j];
+      return F + fo[j];
     }
     const int k = nb - 1 - (j - nb);
-    const long long b = kv.bs[k + 1] - kv.bs[k], bp = kv.bs[k] - kv.bs[k - 1];
+    const long long b = bs[k + 1] - bs[k], bp = bs[k] - bs[k - 1];
     elems = kkt_pad4(b * bp);
-    return kv.F + kv.bo[k];
+    return F + bo[k];
   };
   auto slot = [&](int j) { return ring + (size_t)(j % R) * SM; };
 
@@ -395,77 +578,99 @@ __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T*
     }
     if (prof_issue) *prof_issue += (unsigned long long)(clock64() - t0);
   } else if (tid < GT) {
-    // ---- the solve group ----
-    const bool lo = tid < H;
-    const int r = lo ? tid : tid - H;
-    long long tw = 0, tb = 0;
-    const long long t_start = prof ? clock64() : 0;
-    long long t_fwd = 0;
-    auto sync = [&]() {
-      const long long t = prof ? clock64() : 0;
-      kkt_group_sync(GT);
-      if (prof) tb += clock64() - t;
+    // ---- the solve group: Q lanes per block row ----
+    auto group = [&](auto Qc) {
+      constexpr int Q = decltype(Qc)::value;
+      const bool lo = tid < H;
+      const int t = lo ? tid : tid - H;   // thread in its half
+      const int r = t / Q, q = t % Q;     // block row, lane in the row's group
+      long long tw = 0, tb = 0, td = 0;
+      const long long t_start = prof ? clock64() : 0;
+      long long t_fwd = 0;
+      auto sync = [&]() {
+        const long long t0 = prof ? clock64() : 0;
+        kkt_group_sync(GT);
+        if (prof) tb += clock64() - t0;
+      };
+      auto release = [&](int j) {
+        if (tid == 0) kkt_arrive(&pp->empty[j % R]);
+      };
+      // copy j's data: the ring slot, or global memory after a failed wait
+      // (after one failed wait the CTA stops waiting and reads global memory)
+      auto get = [&](int j) -> const T* {
+        long long el;
+        bool ok = !*(volatile int*)&pp->err;
+        if (ok) {
+          const long long t0 = prof ? clock64() : 0;
+          ok = kkt_wait(&pp->bar[j % R], fpar(j));
+          if (prof) tw += clock64() - t0;
+        }
+        if (!ok) {
+          *(volatile int*)&pp->err = 1;
+          atomicMin(&pp->fail, j);
+          return seg(j, el);
+        }
+        return slot(j);
+      };
+      const T* cur = get(0);
+      for (int k = 1; k < nb; k++) {
+        const int s0 = bs[k], b = bs[k + 1] - s0, sp = bs[k - 1], bp = s0 - sp;
+        const int spp = k > 1 ? bs[k - 2] : sp;
+        const T* prev = cur;              // segment k - 1: S_{k-1}^-1 after G_{k-1}
+        cur = get(k);                     // segment k: G_k first
+        if (lo) {
+          const long long t0 = prof_dot ? clock64() : 0;
+          const bool a = r < b;
+          const kkt_val<T> v = kkt_dot_q<Q>(cur, c, n, sp, b, bp, a ? r : 0, q, a);
+          if (a && q == 0) kkt_vsub(c, n, s0 + r, v);
+          if (prof_dot) td += clock64() - t0;
+        } else {
+          const bool a = r < bp;
+          const kkt_val<T> v = kkt_dot_q<Q>(prev + kkt_pad4((long long)bp * (sp - spp)), c, n, sp, bp, bp, a ? r : 0, q, a);
+          if (a && q == 0) kkt_vset(d, n, sp + r, v);
+        }
+        sync();
+        release(k - 1);
+      }
+      {
+        const int s0 = bs[nb - 1], b = bs[nb] - s0;
+        const int bp = nb > 1 ? s0 - bs[nb - 2] : 0;
+        if (lo) {
+          const bool a = r < b;
+          const kkt_val<T> v = kkt_dot_q<Q>(cur + kkt_pad4((long long)b * bp), c, n, s0, b, b, a ? r : 0, q, a);
+          if (a && q == 0) kkt_vset(d, n, s0 + r, v);
+        }
+        sync();
+        release(nb - 1);
+      }
+      if (prof) t_fwd = clock64();
+      for (int u = 0; u + 1 < nb; u++) {
+        const int k = nb - 1 - u;
+        const int s0 = bs[k], b = bs[k + 1] - s0, sp = bs[k - 1], bp = s0 - sp;
+        const T* Gt = get(nb + u);
+        if (lo) {
+          const long long t0 = prof_dot ? clock64() : 0;
+          const bool a = r < bp;
+          const kkt_val<T> v = kkt_dot_q<Q>(Gt, d, n, s0, bp, b, a ? r : 0, q, a);
+          if (a && q == 0) kkt_vsub(d, n, sp + r, v);
+          if (prof_dot) td += clock64() - t0;
+        } else {
+          if (t < b) xout(perm[s0 + t], kkt_vget(d, n, s0 + t));
+        }
+        sync();
+        release(nb + u);
+      }
+      for (int i = tid; i < bs[1]; i += GT) xout(perm[i], kkt_vget(d, n, i));
+      if (prof) {
+        const long long t_end = clock64();
+        prof[0] += (unsigned long long)tw; prof[1] += (unsigned long long)tb;
+        if (prof_dot) *prof_dot += (unsigned long long)td;
+        prof[2] += (unsigned long long)(t_fwd - t_start); prof[3] += (unsigned long long)(t_end - t_fwd);
+      }
     };
-    auto release = [&](int j) {
-      if (tid == 0) kkt_arrive(&pp->empty[j % R]);
-    };
-    // copy j's data: the ring slot, or global memory after a failed wait
-    // (after one failed wait the CTA stops waiting and reads global memory)
-    auto get = [&](int j) -> const T* {
-      long long el;
-      bool ok = !*(volatile int*)&pp->err;
-      if (ok) {
-        const long long t = prof ? clock64() : 0;
-        ok = kkt_wait(&pp->bar[j % R], fpar(j));
-        if (prof) tw += clock64() - t;
-      }
-      if (!ok) {
-        *(volatile int*)&pp->err = 1;
-        atomicMin(&pp->fail, j);
-        return seg(j, el);
-      }
-      return slot(j);
-    };
-    const T* cur = get(0);
-    for (int k = 1; k < nb; k++) {
-      const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
-      const int spp = k > 1 ? kv.bs[k - 2] : sp;
-      const T* prev = cur;              // segment k - 1: S_{k-1}^-1 after G_{k-1}
-      cur = get(k);                     // segment k: G_k first
-      if (lo) {
-        if (r < b) c[s0 + r] -= kkt_col_dot(cur, c + sp, b, bp, r);
-      } else {
-        if (r < bp) d[sp + r] = kkt_col_dot(prev + kkt_pad4((long long)bp * (sp - spp)), c + sp, bp, bp, r);
-      }
-      sync();
-      release(k - 1);
-    }
-    {
-      const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
-      const int bp = nb > 1 ? s0 - kv.bs[nb - 2] : 0;
-      if (lo && r < b) d[s0 + r] = kkt_col_dot(cur + kkt_pad4((long long)b * bp), c + s0, b, b, r);
-      sync();
-      release(nb - 1);
-    }
-    if (prof) t_fwd = clock64();
-    for (int t = 0; t + 1 < nb; t++) {
-      const int k = nb - 1 - t;
-      const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
-      const T* Gt = get(nb + t);
-      if (lo) {
-        if (r < bp) d[sp + r] -= kkt_col_dot(Gt, d + s0, bp, b, r);
-      } else {
-        if (r < b) xout(kv.perm[s0 + r], d[s0 + r]);
-      }
-      sync();
-      release(nb + t);
-    }
-    for (int i = tid; i < kv.bs[1]; i += GT) xout(kv.perm[i], d[i]);
-    if (prof) {
-      const long long t_end = clock64();
-      prof[0] += (unsigned long long)tw; prof[1] += (unsigned long long)tb;
-      prof[2] += (unsigned long long)(t_fwd - t_start); prof[3] += (unsigned long long)(t_end - t_fwd);
-    }
+    if (QL == 4) group(std::integral_constant<int, 4>{});
+    else if (QL == 2) group(std::integral_constant<int, 2>{});
+    else group(std::integral_constant<int, 1>{});
   }
   __syncthreads();
   if (tid == 0) {
@@ -506,41 +711,66 @@ __device__ void kkt_solve_pipe(const KktView<T>& kv, KktPipe* pp, T* c, T* d, T*
 // the CTA call it; the solve group of kkt_solve_pipe does the block steps.
 template <typename T, typename XO>
 __device__ void kkt_solve(const KktView<T>& kv, T* c, T* d, XO xout) {
-  const int H = kkt_half(kv.bmax), GT = 2 * H;
+  // the view's fields as locals: kv lives in memory that the stores through
+  // the generic solve-vector pointers could alias, so every use would reload it
+  const int* const bs = kv.bs;
+  const int* const fo = kv.fo;
+  const int* const bo = kv.bo;
+  const int* const perm = kv.perm;
+  const T* const F = kv.F;
+  const int QL = kkt_lanes(kv.bmax, blockDim.x);
+  const int H = kkt_group_half(kv.bmax, QL), GT = 2 * H;
   const int tid = threadIdx.x;
-  const int nb = kv.nb;
-  if (tid < GT) {
+  const int nb = kv.nb, n = bs[nb];
+  auto group = [&](auto Qc) {
+    constexpr int Q = decltype(Qc)::value;
     const bool lo = tid < H;
-    const int r = lo ? tid : tid - H;
+    const int t = lo ? tid : tid - H;
+    const int r = t / Q, q = t % Q;
     // forward: c_k -= G_k c_{k-1} (lower half) while d_{k-1} = S_{k-1}^-1 c_{k-1} (upper half)
     for (int k = 1; k < nb; k++) {
-      const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
-      const int spp = k > 1 ? kv.bs[k - 2] : sp;
+      const int s0 = bs[k], b = bs[k + 1] - s0, sp = bs[k - 1], bp = s0 - sp;
+      const int spp = k > 1 ? bs[k - 2] : sp;
       if (lo) {
-        if (r < b) c[s0 + r] -= kkt_col_dot(kv.F + kv.fo[k], c + sp, b, bp, r);
+        const bool a = r < b;
+        const kkt_val<T> v = kkt_dot_q<Q>(F + fo[k], c, n, sp, b, bp, a ? r : 0, q, a);
+        if (a && q == 0) kkt_vsub(c, n, s0 + r, v);
       } else {
-        if (r < bp)
-          d[sp + r] = kkt_col_dot(kv.F + kv.fo[k - 1] + kkt_pad4((long long)bp * (sp - spp)), c + sp, bp, bp, r);
+        const bool a = r < bp;
+        const kkt_val<T> v =
+            kkt_dot_q<Q>(F + fo[k - 1] + kkt_pad4((long long)bp * (sp - spp)), c, n, sp, bp, bp, a ? r : 0, q, a);
+        if (a && q == 0) kkt_vset(d, n, sp + r, v);
       }
       kkt_group_sync(GT);
     }
     {
-      const int s0 = kv.bs[nb - 1], b = kv.bs[nb] - s0;
-      const int bp = nb > 1 ? s0 - kv.bs[nb - 2] : 0;
-      if (lo && r < b) d[s0 + r] = kkt_col_dot(kv.F + kv.fo[nb - 1] + kkt_pad4((long long)b * bp), c + s0, b, b, r);
+      const int s0 = bs[nb - 1], b = bs[nb] - s0;
+      const int bp = nb > 1 ? s0 - bs[nb - 2] : 0;
+      if (lo) {
+        const bool a = r < b;
+        const kkt_val<T> v = kkt_dot_q<Q>(F + fo[nb - 1] + kkt_pad4((long long)b * bp), c, n, s0, b, b, a ? r : 0, q, a);
+        if (a && q == 0) kkt_vset(d, n, s0 + r, v);
+      }
       kkt_group_sync(GT);
     }
     // backward: x_{k-1} = d_{k-1} - G_k' x_k (lower half) while block k is written out (upper half)
     for (int k = nb - 1; k >= 1; k--) {
-      const int s0 = kv.bs[k], b = kv.bs[k + 1] - s0, sp = kv.bs[k - 1], bp = s0 - sp;
+      const int s0 = bs[k], b = bs[k + 1] - s0, sp = bs[k - 1], bp = s0 - sp;
       if (lo) {
-        if (r < bp) d[sp + r] -= kkt_col_dot(kv.F + kv.bo[k], d + s0, bp, b, r);
+        const bool a = r < bp;
+        const kkt_val<T> v = kkt_dot_q<Q>(F + bo[k], d, n, s0, bp, b, a ? r : 0, q, a);
+        if (a && q == 0) kkt_vsub(d, n, sp + r, v);
       } else {
-        if (r < b) xout(kv.perm[s0 + r], d[s0 + r]);
+        if (t < b) xout(perm[s0 + t], kkt_vget(d, n, s0 + t));
       }
       kkt_group_sync(GT);
     }
-    for (int i = tid; i < kv.bs[1]; i += GT) xout(kv.perm[i], d[i]);
+    for (int i = tid; i < bs[1]; i += GT) xout(perm[i], kkt_vget(d, n, i));
+  };
+  if (tid < GT) {
+    if (QL == 4) group(std::integral_constant<int, 4>{});
+    else if (QL == 2) group(std::integral_constant<int, 2>{});
+    else group(std::integral_constant<int, 1>{});
   }
   __syncthreads();
 }

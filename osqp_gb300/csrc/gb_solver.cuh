@@ -643,20 +643,28 @@ struct Solver {
     // the dense-row form leaves its dense rows out of the right-hand side (they
     // enter its solve through z - rho^-1 y, dr_solve)
     const int* const ddx = pr.kkt.dr > 0 ? pr.kkt.didx : nullptr;
+    // the vectors as locals (not reloaded from the problem struct per row)
+    const T* const qv = pr.q;
+    const T* const rv = pr.rho_vec;
+    const T* const riv = pr.rho_inv_vec;
+    T* const rhsv = pr.rhs;
     rows_auto(g, span_n(g, n), pr.At,
       [&](int j) {
         if (direct) return (ddx && ddx[j] >= 0) ? T(0) : kw[j];
-        const T rj = vec ? pr.rho_vec[j] : rho_s;
-        const T ij = vec ? pr.rho_inv_vec[j] : rinv_s;
+        const T rj = vec ? rv[j] : rho_s;
+        const T ij = vec ? riv[j] : rinv_s;
         return rj * (z[j] - ij * y[j]);
       },
       [&](int i, T v) {
-        const T b1 = sig * x[i] - pr.q[i];
+        const T b1 = sig * x[i] - qv[i];
         const T rr = b1 + v;
         if (direct) {
-          kc[kip ? kip[i] : i] = rr;
+          // the block form's solve vector (double-float in the FP64 build);
+          // the dense-row form reads plain values
+          if (ddx) kc[kip ? kip[i] : i] = rr;
+          else kkt_vput(kc, n, kip ? kip[i] : i, rr);
         } else {
-          pr.rhs[i] = rr;
+          rhsv[i] = rr;
           mx0[0] = tmax(mx0[0], (T)fabs(rr));   // the PCG's tolerance only
         }
       });
@@ -723,10 +731,10 @@ struct Solver {
         const bool piped = pr.kkt.ring >= 2 && pr.kpipe;
         if (piped)
           kkt_solve_pipe<T>(pr.kkt, pr.kpipe, kc, kc + n, kc + kkt_pad4(2LL * n),
-                            [&](int i, T v) { kxs[i] = v; }, prof ? sc->prof + 5 : nullptr,
-                            s.profile ? sc->prof + 11 : nullptr);
+                            [kxs](int i, T v) { kxs[i] = v; }, prof ? sc->prof + 5 : nullptr,
+                            s.profile ? sc->prof + 11 : nullptr, prof ? sc->prof + 15 : nullptr);
         else
-          kkt_solve<T>(pr.kkt, kc, kc + n, [&](int i, T v) { kxs[i] = v; });
+          kkt_solve<T>(pr.kkt, kc, kc + n, [kxs](int i, T v) { kxs[i] = v; });
         if (prof) {
           sc->prof[12] += 1;
           if (piped) { sc->prof[13] += 1; if (pr.kpipe->err) sc->prof[14] += 1; }
@@ -753,16 +761,20 @@ struct Solver {
     });
     if (prof) { const long long t = clock64(); sc->prof[2] += (unsigned long long)(t - pt); pt = t; }
     if (m > 0) {
+      // the vectors as locals (not reloaded from the problem struct per row)
+      const T* const lv = pr.l;
+      const T* const uv = pr.u;
+      T* const dyv = pr.dy;
       rows_auto(g, span_m(g, m), pr.A, [&](int c) { return direct ? kxs[c] : xp[c]; }, [&](int j, T zt) {
-        const T ri = vec ? pr.rho_inv_vec[j] : rinv_s;
-        const T rr = vec ? pr.rho_vec[j] : rho_s;
+        const T ri = vec ? riv[j] : rinv_s;
+        const T rr = vec ? rv[j] : rho_s;
         const T zo = z[j];
         const T zr = al * zt + oma * zo;
         const T zz = zr + ri * y[j];
-        const T zn = tmin(tmax(zz, pr.l[j]), pr.u[j]);
+        const T zn = tmin(tmax(zz, lv[j]), uv[j]);
         const T d = rr * (zr - zn);
         z[j] = zn;
-        pr.dy[j] = d;
+        dyv[j] = d;
         y[j] = y[j] + d;
       });
     }
@@ -1111,6 +1123,17 @@ struct Solver {
     typedef typename K::I I;
     const I inf_gt = K::thr_gt(infval), inf_lt = K::thr_lt(infval), dz_lt = K::thr_lt(s.zero_deadzone);
 
+    // the vectors as locals (not reloaded from the problem struct per row)
+    const T* const lv = pr.l;
+    const T* const uv = pr.u;
+    const T* const Ev = pr.E;
+    const T* const Eiv = pr.Einv;
+    T* const dyv = pr.dy;
+    const T* const dxv = pr.dx;
+    const T* const qv = pr.q;
+    const T* const Dv = pr.D;
+    const T* const Div = pr.Dinv;
+
     // Phase T1 over the rows of A: Ax, A dx and the m-length terms.
     // mx: 0 |Ax-z|  1 |Einv(Ax-z)|  2 |z|  3 |Ax|  4 |Einv z|  5 |Einv Ax|
     //     6 |dy_proj| (|E dy_proj| for unscaled termination)
@@ -1122,10 +1145,10 @@ struct Solver {
     for (int k = 0; k < 7; k++) km[k] = 0;
     km[7] = K::key(T(-INFINITY));
     if (m > 0) {
-      rows_auto2(g, span_m(g, m), pr.A, [&](int c) { return x[c]; }, [&](int c) { return pr.dx[c]; },
+      rows_auto2(g, span_m(g, m), pr.A, [&](int c) { return x[c]; }, [&](int c) { return dxv[c]; },
         [&](int j, T ax, T adx) {
-          const T l = pr.l[j], u = pr.u[j];
-          const T ei = pr.Einv[j];
+          const T l = lv[j], u = uv[j];
+          const T ei = Eiv[j];
           const T zj = z[j];
           const T pres = ax - zj;
           km[0] = umaxk(km[0], K::absk(pres));
@@ -1144,11 +1167,11 @@ struct Solver {
           sm[0].add_prod(u, K::pos(yp));
           sm[0].add_prod(l, K::neg(yp));
           // project dy onto the polar recession cone (in place) (auxil.c:476-480)
-          T dp = pr.dy[j];
+          T dp = dyv[j];
           if (u_inf) dp = l_inf ? T(0) : K::neg(dp);
           else if (l_inf) dp = K::pos(dp);
-          pr.dy[j] = dp;
-          km[6] = umaxk(km[6], K::absk(uns ? pr.E[j] * dp : dp));
+          dyv[j] = dp;
+          km[6] = umaxk(km[6], K::absk(uns ? Ev[j] * dp : dp));
           sm[1].add_prod(u, K::pos(dp));
           sm[1].add_prod(l, K::neg(dp));
           // recession cone test of A dx (vector.c:704-727): violation if
@@ -1177,8 +1200,8 @@ struct Solver {
     for (int k = 0; k < 11; k++) k2[k] = 0;
     {
       auto fn = [&](int i, T px, T pdx, T aty, T atdy) {
-        const T q = pr.q[i];
-        const T di = pr.Dinv[i];
+        const T q = qv[i];
+        const T di = Div[i];
         const T dr = (m > 0) ? (q + px) + aty : q + px;
         k2[0] = umaxk(k2[0], K::absk(dr));
         k2[1] = umaxk(k2[1], K::absk(di * dr));
@@ -1188,8 +1211,8 @@ struct Solver {
         k2[5] = umaxk(k2[5], K::absk(di * q));
         k2[6] = umaxk(k2[6], K::absk(di * aty));
         k2[7] = umaxk(k2[7], K::absk(di * px));
-        const T dxi = pr.dx[i];
-        k2[8] = umaxk(k2[8], K::absk(uns ? pr.D[i] * dxi : dxi));
+        const T dxi = dxv[i];
+        k2[8] = umaxk(k2[8], K::absk(uns ? Dv[i] * dxi : dxi));
         k2[9] = umaxk(k2[9], K::absk(uns ? pdx * di : pdx));
         k2[10] = umaxk(k2[10], K::absk(uns ? atdy * di : atdy));
         s2[0].add_prod(px, x[i]);
@@ -1197,9 +1220,9 @@ struct Solver {
         s2[2].add_prod(q, dxi);
       };
       auto xp1 = [&](int c) { return x[c]; };
-      auto xp2 = [&](int c) { return pr.dx[c]; };
+      auto xp2 = [&](int c) { return dxv[c]; };
       auto xa1 = [&](int c) { return y[c]; };
-      auto xa2 = [&](int c) { return pr.dy[c]; };
+      auto xa2 = [&](int c) { return dyv[c]; };
       const Rng rg = span_n(g, n);
       const int L = kktL;
       if constexpr (std::is_same<G, GridGroup>::value || !std::is_same<T, double>::value) {
