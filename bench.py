@@ -91,9 +91,9 @@ def make_workload(count, steps, seed=3, share=0):
 # DRAM bytes per algorithmic byte of the solve launch, from one ncu capture
 # of a smaller batch of the same QPs (the 4096-QP launch is too long to
 # capture); the launch's traffic is this ratio times its algorithmic bytes.
-# Direct solver, FP64: 304 QPs, 89.39 + 12.51 GB DRAM for 108.06 GB
+# Direct solver, FP64: 304 QPs, 65.54 + 2.67 GB DRAM for 108.06 GB
 # algorithmic.  The PCG path and the FP32 direct path are not captured.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {("direct", "f64"): (89.385127 + 12.505955) / 108.057547680}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {("direct", "f64"): (65.542542 + 2.668631) / 108.057547680}
 
 
 def measured_peak():
