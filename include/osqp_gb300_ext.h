@@ -104,6 +104,19 @@ OSQPInt osqp_gb300_batch_setup(OSQPBatch** batchp, OSQPInt count, const OSQPInt*
 OSQPInt osqp_gb300_batch_update_data_vec(OSQPBatch* batch, const OSQPFloat* q, const OSQPFloat* l,
                                          const OSQPFloat* u);
 
+/* New values of QP k's P entries (upper triangle, in the order given at setup)
+ * and A entries; replaces osqp_update_data_mat (include/public/osqp_api_functions.h,
+ * src/osqp_api.c:1309-1409) for one QP of a batch, with its arguments: NULL
+ * values leave a matrix unchanged, NULL indices with a count of 0 or of all
+ * entries update every entry in order.  Returns 1 / 2 for a bad P / A count
+ * (as the reference), OSQP_DATA_VALIDATION_ERROR for k or an index out of
+ * range (nothing changed).  QP k is re-scaled and refactored (direct solver)
+ * or its preconditioner rebuilt, with rho and its iterates kept.  A pool of a
+ * server may be updated while none of its requests is in flight. */
+OSQPInt osqp_gb300_batch_update_data_mat(OSQPBatch* batch, OSQPInt k, const OSQPFloat* Px_new,
+                                         const OSQPInt* Px_new_idx, OSQPInt P_new_n, const OSQPFloat* Ax_new,
+                                         const OSQPInt* Ax_new_idx, OSQPInt A_new_n);
+
 /* Solve all QPs (cold or warm start per settings->warm_starting). */
 OSQPInt osqp_gb300_batch_solve(OSQPBatch* batch);
 

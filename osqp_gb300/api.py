@@ -338,6 +338,8 @@ class Batch:
         L.osqp_gb300_batch_setup.restype = I
         L.osqp_gb300_batch_update_data_vec.argtypes = [C.c_void_p, PF, PF, PF]
         L.osqp_gb300_batch_update_data_vec.restype = I
+        L.osqp_gb300_batch_update_data_mat.argtypes = [C.c_void_p, I, PF, PI, I, PF, PI, I]
+        L.osqp_gb300_batch_update_data_mat.restype = I
         L.osqp_gb300_batch_solve.argtypes = [C.c_void_p]
         L.osqp_gb300_batch_solve.restype = I
         L.osqp_gb300_batch_get_solution.argtypes = [C.c_void_p, PF, PF, PI, PI, PF, PF, PF]
@@ -401,6 +403,19 @@ class Batch:
         conv = lambda v: None if v is None else np.ascontiguousarray(v, dtype=fdt)
         qa, la, ua = conv(q), conv(l), conv(u)
         return int(self.L.lib.osqp_gb300_batch_update_data_vec(self._h, _ptr(qa, F), _ptr(la, F), _ptr(ua, F)))
+
+    def update_mat(self, k: int, Px=None, Px_idx=None, Ax=None, Ax_idx=None) -> int:
+        """New P (upper triangle) / A values of QP k, as osqp_update_data_mat
+        (src/osqp_api.c:1309-1409): values in the entry order of set-up, or at
+        the given entry indices."""
+        L = self.L
+        fdt, idt = L.np_float, np.int64 if C.sizeof(L.I) == 8 else np.int32
+        conv = lambda v, t: None if v is None else np.ascontiguousarray(v, dtype=t)
+        pa, pi, aa, ai = conv(Px, fdt), conv(Px_idx, idt), conv(Ax, fdt), conv(Ax_idx, idt)
+        pn = 0 if pa is None else (pi.size if pi is not None else pa.size)
+        an = 0 if aa is None else (ai.size if ai is not None else aa.size)
+        return int(L.lib.osqp_gb300_batch_update_data_mat(self._h, int(k), _ptr(pa, L.F), _ptr(pi, L.I), pn,
+                                                          _ptr(aa, L.F), _ptr(ai, L.I), an))
 
     def solve(self) -> int:
         return int(self.L.lib.osqp_gb300_batch_solve(self._h))

@@ -141,7 +141,7 @@ struct BatchArrays {
   }
 };
 
-enum BatchMode : int { kModeSetup = 0, kModeSolve = 1, kModeUpdateVec = 2 };
+enum BatchMode : int { kModeSetup = 0, kModeSolve = 1, kModeUpdateVec = 2, kModeUpdateMat = 3 };
 
 // Shared-memory staging of one QP for a solve.
 //
@@ -401,6 +401,12 @@ __device__ void batch_item(G& g, const BatchArrays<TT>& B, const DevSettings& s,
     S.setup(g);
   } else if (mode == kModeSolve) {
     S.solve(g, it_lo, it_hi);
+  } else if (mode == kModeUpdateMat) {
+    // new P / A values already in Praw / Araw (osqp_api.c:1309-1409): values,
+    // scaling (q, l, u re-scaled from their inputs) and preconditioner or
+    // factor; rho and the iterates are kept
+    S.prepare_data(g, true);
+    if (threadIdx.x == 0) { ssc.status = ST_UNSOLVED; ssc.rho_updates = 0; }
   } else {
     // new q / l / u from *_in with the QP's existing scaling (osqp_api.c:1184-1257)
     const TT c = (TT)ssc.c;
@@ -599,6 +605,12 @@ template <typename TT>
 __global__ void k_batch_check_bounds(const TT* l, const TT* u, long long msum, int* bad) {
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < msum; j += (long long)gridDim.x * blockDim.x)
     if (l[j] > u[j]) atomicExch(bad, 1);
+}
+
+template <typename TT>
+__global__ void k_batch_scatter_vals(TT* dst, const TT* src, const int* idx, int cnt) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x)
+    dst[idx ? idx[k] : k] = src[k];
 }
 
 struct BatchInfo { int status, iter; long long pcg; double obj, prim, dual, seconds; int rho_updates, pad; };
@@ -1292,6 +1304,75 @@ extern "C" OSQPInt osqp_gb300_batch_update_data_vec(OSQPBatch* b, const OSQPFloa
   }
   if (q) BT_TRY(cudaMemcpyAsync(B.vn[1], q, sizeof(T) * b->nsum, cudaMemcpyDefault, s));
   int rc = run_batch_kernel(b, kModeUpdateVec);
+  if (rc) return rc;
+  return cudaStreamSynchronize(s) == cudaSuccess ? 0 : OSQP_ALGEBRA_LOAD_ERROR;
+}
+
+// New values of QP k's P (upper triangle, input order) and A entries
+// (osqp_update_data_mat, osqp_api.c:1309-1409).  Return codes as the
+// reference's: 1 / 2 for a bad P / A count.  Indices are checked on the host
+// (an index outside the QP's entries is OSQP_DATA_VALIDATION_ERROR, nothing
+// changed), then one launch re-scales QP k and refactors (direct solver) or
+// rebuilds its preconditioner, keeping rho and the iterates.
+extern "C" OSQPInt osqp_gb300_batch_update_data_mat(OSQPBatch* b, OSQPInt k, const OSQPFloat* Px_new,
+                                                    const OSQPInt* Px_new_idx, OSQPInt P_new_n,
+                                                    const OSQPFloat* Ax_new, const OSQPInt* Ax_new_idx,
+                                                    OSQPInt A_new_n) {
+  if (!b) return OSQP_WORKSPACE_NOT_INIT_ERROR;
+  if (k < 0 || k >= b->count) return OSQP_DATA_VALIDATION_ERROR;
+  const long long nnzP = b->nnzT_k[k], nnzA = b->nnzA_k[k];
+  if (P_new_n > nnzP || P_new_n < 0) return 1;
+  if (!Px_new_idx && P_new_n != 0 && P_new_n != nnzP) return 1;
+  if (P_new_n == 0) P_new_n = (OSQPInt)nnzP;
+  if (A_new_n > nnzA || A_new_n < 0) return 2;
+  if (!Ax_new_idx && A_new_n != 0 && A_new_n != nnzA) return 2;
+  if (A_new_n == 0) A_new_n = (OSQPInt)nnzA;
+  const bool doP = Px_new && P_new_n > 0, doA = Ax_new && A_new_n > 0;
+  if (!doP && !doA) return 0;
+  cudaSetDevice(b->device);
+  cudaStream_t s = b->stream;
+  // indices on the host first: nothing reaches the device unless all are in range
+  std::vector<int> pi, ai;
+  auto fetch_idx = [&](const OSQPInt* idx, OSQPInt cnt, long long lim, std::vector<int>& out) -> bool {
+    if (!idx) return true;
+    std::vector<OSQPInt> h(cnt);
+    if (cudaMemcpy(h.data(), idx, sizeof(OSQPInt) * cnt, cudaMemcpyDefault) != cudaSuccess) return false;
+    out.resize(cnt);
+    for (OSQPInt i = 0; i < cnt; i++) {
+      if (h[i] < 0 || h[i] >= lim) return false;
+      out[i] = (int)h[i];
+    }
+    return true;
+  };
+  if ((doP && !fetch_idx(Px_new_idx, P_new_n, nnzP, pi)) || (doA && !fetch_idx(Ax_new_idx, A_new_n, nnzA, ai)))
+    return OSQP_DATA_VALIDATION_ERROR;
+  const int mx = std::max(doP ? P_new_n : 0, doA ? A_new_n : 0);
+  T* tmpv = nullptr;
+  int* tmpi = nullptr;
+  int* d_k = nullptr;
+  BT_TRY(cudaMallocAsync((void**)&tmpv, sizeof(T) * mx, s));
+  BT_TRY(cudaMallocAsync((void**)&tmpi, sizeof(int) * mx, s));
+  BT_TRY(cudaMallocAsync((void**)&d_k, sizeof(int), s));
+  const BatchInst& I = b->inst[k];
+  const int qk = (int)k;
+  BT_TRY(cudaMemcpyAsync(d_k, &qk, sizeof(int), cudaMemcpyHostToDevice, s));
+  if (doP) {
+    BT_TRY(cudaMemcpyAsync(tmpv, Px_new, sizeof(T) * P_new_n, cudaMemcpyDefault, s));
+    if (Px_new_idx) BT_TRY(cudaMemcpyAsync(tmpi, pi.data(), sizeof(int) * P_new_n, cudaMemcpyHostToDevice, s));
+    k_batch_scatter_vals<T><<<64, 256, 0, s>>>(b->B.Praw + I.pt_off, tmpv, Px_new_idx ? tmpi : nullptr, P_new_n);
+    BT_TRY(cudaGetLastError());
+  }
+  if (doA) {
+    BT_TRY(cudaMemcpyAsync(tmpv, Ax_new, sizeof(T) * A_new_n, cudaMemcpyDefault, s));
+    if (Ax_new_idx) BT_TRY(cudaMemcpyAsync(tmpi, ai.data(), sizeof(int) * A_new_n, cudaMemcpyHostToDevice, s));
+    k_batch_scatter_vals<T><<<64, 256, 0, s>>>(b->B.Araw + I.a_off, tmpv, Ax_new_idx ? tmpi : nullptr, A_new_n);
+    BT_TRY(cudaGetLastError());
+  }
+  LaunchBufs lb{d_k, 1, b->d_queue2, b->d_order2};
+  const int rc = launch_batch(b, kModeUpdateMat, lb, s, false);
+  cudaFreeAsync(tmpv, s);
+  cudaFreeAsync(tmpi, s);
+  cudaFreeAsync(d_k, s);
   if (rc) return rc;
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : OSQP_ALGEBRA_LOAD_ERROR;
 }
