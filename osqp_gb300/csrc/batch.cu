@@ -665,7 +665,8 @@ static int env_int(const char* name, int dflt);
 // (one box, alternating): the PCG runs 1024 x 1 (512 x 2: -7 %); the direct
 // solver runs 512 x 1 (against 1024 x 1: +4.7 % FP64, +6.7 % FP32; its block
 // solve uses a few warps, and the sparse products of the FP64 build are bound
-// by the FP64 pipe rather than by the number of warps).
+// by the FP64 pipe rather than by the number of warps; 768 x 1, 80 registers,
+// 8 lanes per block row: -25 % FP64, -2.5 % FP32).
 static void cta_form(bool direct, BatchKernel* fn, int* nt, int* minb) {
   const int threads = env_int("OSQP_GB300_BATCH_THREADS", direct ? 512 : 1024);
   const int per_sm = env_int("OSQP_GB300_BATCH_CTAS_PER_SM", direct ? 1 : 2);
