@@ -760,6 +760,11 @@ def main():
                                            "kind": "port", "sample": cpu["sample"]},
         clocks=g["clocks"], gpu_launches=g["launches"],
         linsys_solver="direct (block-tridiagonal LDL')" if direct else "indirect (reduced-KKT PCG)",
+        arithmetic=("FP64; the direct solver factors in FP64 and runs its block solve in double-float "
+                    "(hi + lo floats, 48 significant bits) on the FP32 pipe"
+                    if direct and args.precision == "f64" else
+                    "FP64" if args.precision == "f64" else
+                    "FP32 iterates and factors, double-float reductions, FP64 scalars"),
         plain_gpu_solves_per_s=g["plain"],
         batched_over_plain=(g["value"] / g["plain"]) if g["plain"] else None,
         admm_iters_per_qp=g["admm_per_qp"], pcg_iters_per_qp=g["pcg_per_qp"],
