@@ -218,8 +218,10 @@ OSQPInt osqp_gb300_kkt_plan(OSQPInt n, OSQPInt m, const OSQPInt* Pp, const OSQPI
  * one pool (at most one per QP at a time, at most the pool's resident CTA
  * slots / concurrency) as one launch, so work from different arrivals
  * overlaps on the device.  A request's result is the same whatever
- * else is in flight.  A pool served by a server must not be used through the
- * batch calls meanwhile. */
+ * else is in flight.  Pools may be added while the server runs: a QP of a
+ * structure no pool holds is admitted by setting it up as a one-QP pool (the
+ * per-request counterpart of osqp_setup).  A pool served by a server must not
+ * be used through the batch calls while any of its requests is in flight. */
 typedef struct OSQPServer_ OSQPServer;
 
 OSQPInt osqp_gb300_server_create(OSQPServer** server, OSQPInt concurrency);

@@ -117,3 +117,45 @@ def test_pool_admission_by_free_memory():
     b = Batch(lib)
     assert b.setup(probs, **SERVE) == 0
     assert b.solve() == 0
+
+
+def test_new_structure_admitted_while_serving(oracle_lib):
+    """A QP of a structure no pool holds is admitted while requests are in
+    flight: set up as a one-QP pool and added to the running server (the
+    per-request counterpart of osqp_setup, src/osqp_api.c:332-631).  Its
+    results meet the oracle's bars, and a matrix update of that pool between
+    its requests (osqp_gb300_batch_update_data_mat) is served with the new
+    values."""
+    from osqp_gb300.api import DIRECT_SOLVER, OSQP
+    lib = load("f64")
+    st = dict(SERVE, linsys_solver=DIRECT_SOLVER)
+    probs = pb.mpc_batch(6, seed=40)
+    pool = Batch(lib)
+    assert pool.setup(probs, **st) == 0
+    srv = Server(lib, concurrency=3)
+    pid = srv.add_pool(pool)
+    busy = [srv.submit(pid, k) for k in range(len(probs))]          # requests in flight
+    new = pb.mpc(np.random.default_rng(41))
+    one = Batch(lib)
+    assert one.setup([new], **st) == 0
+    nid = srv.add_pool(one)                                          # admitted while serving
+    x, status, it, obj, lat = srv.wait(srv.submit(nid, 0), new[0].shape[0])
+    o = OSQP(oracle_lib)
+    assert o.setup(*new, **st) == 0
+    r = o.solve()
+    assert status == r.info["status_val"] == SOLVED
+    assert abs(objective(new[0], new[1], x) - r.info["obj_val"]) <= 1e-7 * max(1.0, abs(r.info["obj_val"]))
+    assert it == r.info["iter"]
+    for k, t in enumerate(busy):
+        srv.wait(t, probs[k][0].shape[0])
+    # new A values for the admitted QP, between its requests
+    A = new[2].tocsc()
+    ax = A.data * 1.03
+    assert one.update_mat(0, Ax=ax) == 0
+    assert o.update(Ax=ax) == 0
+    x, status, it, obj, lat = srv.wait(srv.submit(nid, 0), new[0].shape[0])
+    r = o.solve()
+    assert status == r.info["status_val"] == SOLVED
+    assert abs(objective(new[0], new[1], x) - r.info["obj_val"]) <= 1e-7 * max(1.0, abs(r.info["obj_val"]))
+    assert it == r.info["iter"]
+    srv.close()
