@@ -17,11 +17,12 @@
 // same x~ and z~ in exact arithmetic).
 //
 // A solve is a chain of dependent block steps, each a few small dense
-// products, so it runs on a small group of warps (two halves of kkt_half(bmax)
-// threads, one thread per block row, column-major blocks so that the threads
-// of a step read consecutive words) synchronised by a named barrier; the other
-// warps of the CTA wait once at the end instead of taking every step's
-// barrier.  The factor streams through shared memory: each block's segment
+// products, so it runs on a group of warps (two halves, Q lanes per block row,
+// column-major blocks so that the lanes of a step read consecutive words)
+// synchronised by a named barrier; the other warps of the CTA wait once at the
+// end instead of taking every step's barrier.  The FP64 build stores the
+// factor as double-float pairs and runs the block products on the FP32 pipe
+// (see kKktDF below).  The factor streams through shared memory: each block's segment
 // (gb_kkt_plan.h) is one bulk copy (cp.async.bulk, the TMA engine's untiled
 // form) into a ring of `ring` slots, issued by a producer warp outside the
 // group and tracked by a "full" mbarrier per slot; the group hands a slot back
