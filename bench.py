@@ -94,6 +94,11 @@ def make_workload(count, steps, seed=3, share=0):
 # Direct solver, FP64: 304 QPs, 65.54 + 2.67 GB DRAM for 108.06 GB
 # algorithmic.  The PCG path and the FP32 direct path are not captured.
 TRAFFIC_PER_ALGORITHMIC_BYTE = {("direct", "f64"): (65.542542 + 2.668631) / 108.057547680}
+# The same for the single large sparse QP (PCG, grid form), from one ncu
+# capture of each precision's timed solve: FP32 45.03 + 6.93 MB DRAM for
+# 31.22 GB algorithmic (the QP stays in L2), FP64 16.09 + 4.51 GB for 19.41 GB.
+TRAFFIC_SINGLE = {("large_sparse", "f32"): (45.033472e6 + 6.934528e6) / 31.22e9,
+                  ("large_sparse", "f64"): (16.087259e9 + 4.507228e9) / 19.41e9}
 
 
 def measured_peak():
@@ -520,7 +525,11 @@ def single_config_result(which, oracle_timeout):
             "admm_iters_per_s": stt["admm_iter"] / (kms * 1e-3), "pcg_iters_per_s": stt["pcg_iter"] / (kms * 1e-3),
             "execution_form": {0: "cta", 1: "grid"}.get(stt["grid"], f"cluster{stt['grid']}"),
             "roofline": {"bound": "hbm", "achieved": byt / (kms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": byt / (kms * 1e-3) / 1e9 / peak, "peak_source": peak_kind},
+                         "frac": byt / (kms * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
+                         "traffic": (TRAFFIC_SINGLE[(which, prec)] * byt) if (which, prec) in TRAFFIC_SINGLE else None,
+                         "traffic_source": ("ncu capture of this solve (dram read+write / algorithmic bytes = "
+                                            f"{TRAFFIC_SINGLE[(which, prec)]:.4f})")
+                         if (which, prec) in TRAFFIC_SINGLE else "not captured"},
             "obj": obj, "prim_res": prim, "dual_res": dual}
         solver.cleanup()
     if oracle_timeout > 0:
